@@ -1,0 +1,680 @@
+// Host side of the f(A)b engine: argument checks, CSC/CSR -> SELL-32
+// conversion, device allocation, cooperative launches and the C ABI declared
+// in include/gpumatfun.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "../../include/gpumatfun.h"
+#include "fab_kernel.cuh"
+
+using gm::KParams;
+
+namespace gm {
+void* kernel_fp64(int R, int group);
+void* kernel_mixed(int R, int group);
+}  // namespace gm
+
+namespace {
+
+thread_local std::string g_create_error;
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct gm_engine {
+  int dev = 0, nsm = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  long long n = 0, nnz = 0, nslices = 0, padded = 0;
+  int R = 0, m = 0, d = 0, C = 0, k = 0, prec = 0, sync_mode = 1;
+  int threads = 512, G = 0;
+  int Gk[5] = {};                // grid size per phase group (co-residency bound)
+  void* kfn[5] = {};
+  std::vector<DevBuf> bufs;
+  size_t bytes = 0;
+  KParams kp{};
+  double* stage = nullptr;       // n*R column-major staging for host transfers
+  double* col_scale = nullptr;   // device, R
+  int* h_status = nullptr;       // pinned: [0] status, [1..R] meff
+  cudaEvent_t ev[5][2] = {};
+  bool ev_used[5] = {};
+  bool have_y = false, have_coef = false, have_V = false;
+  long long launches = 0;
+  std::string err;
+};
+
+namespace {
+
+int fail(gm_engine* e, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (e) e->err = buf; else g_create_error = buf;
+  return code;
+}
+
+int cuda_fail(gm_engine* e, cudaError_t st, const char* what) {
+  return fail(e, GM_ERR_CUDA, "%s: %s", what, cudaGetErrorString(st));
+}
+
+#define GM_CUDA(e, call)                                   \
+  do {                                                     \
+    cudaError_t _st = (call);                              \
+    if (_st != cudaSuccess) return cuda_fail((e), _st, #call); \
+  } while (0)
+
+template <class T>
+int dalloc(gm_engine* e, T** p, size_t count) {
+  size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+  void* q = nullptr;
+  cudaError_t st = cudaMalloc(&q, bytes);
+  if (st != cudaSuccess) {
+    cudaGetLastError();
+    return fail(e, GM_ERR_OOM, "device allocation of %zu bytes failed: %s", bytes, cudaGetErrorString(st));
+  }
+  e->bufs.push_back({q, bytes});
+  e->bytes += bytes;
+  *p = reinterpret_cast<T*>(q);
+  return GM_OK;
+}
+
+template <class T>
+int dupload(gm_engine* e, T** p, const T* host, size_t count) {
+  int rc = dalloc(e, p, count);
+  if (rc) return rc;
+  if (count) GM_CUDA(e, cudaMemcpy(*p, host, count * sizeof(T), cudaMemcpyHostToDevice));
+  return GM_OK;
+}
+
+// ------------------------------------------------------------------ helper kernels
+__global__ void k_pack_in(const double* __restrict__ cm, double* __restrict__ il, long long n, int R,
+                          const double* __restrict__ scale) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * R) return;
+  const long long i = t / R;
+  const int r = (int)(t % R);
+  il[t] = cm[(long long)r * n + i] * scale[r];
+}
+
+__global__ void k_pack_out(const double* __restrict__ il, double* __restrict__ cm, long long n, int R) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * R) return;
+  const long long i = t / R;
+  const int r = (int)(t % R);
+  cm[(long long)r * n + i] = il[t];
+}
+
+// ------------------------------------------------------------------ sparse conversion
+struct Csr {
+  std::vector<long long> ptr;
+  std::vector<int> col;
+  std::vector<double> val;
+};
+
+int make_csr(gm_engine* e, const gm_create_args* a, Csr& out) {
+  const long long n = a->n;
+  const long long* ptr = reinterpret_cast<const long long*>(a->ptr);
+  const long long* ind = reinterpret_cast<const long long*>(a->ind);
+  if (ptr[0] != 0) return fail(e, GM_ERR_ARG, "lanczos_create:inputNotSparse: pointer array must start at 0");
+  for (long long i = 0; i < n; ++i)
+    if (ptr[i + 1] < ptr[i]) return fail(e, GM_ERR_ARG, "lanczos_create:inputNotSparse: pointer array not monotone at %lld", i);
+  const long long nnz = ptr[n];
+  if (a->nnz && a->nnz < nnz) return fail(e, GM_ERR_ARG, "lanczos_create:inputNotSparse: nnz %lld < ptr[n] %lld", (long long)a->nnz, nnz);
+  if (nnz > 2147483647LL) return fail(e, GM_ERR_UNSUPPORTED, "more than 2^31-1 stored entries");
+  for (long long t = 0; t < nnz; ++t)
+    if (ind[t] < 0 || ind[t] >= n) return fail(e, GM_ERR_ARG, "lanczos_create:inputNotSparse: index %lld out of range at %lld", (long long)ind[t], t);
+  out.ptr.assign(n + 1, 0);
+  out.col.resize(nnz);
+  out.val.resize(nnz);
+  if (a->format == GM_CSR) {
+    for (long long i = 0; i <= n; ++i) out.ptr[i] = ptr[i];
+    for (long long t = 0; t < nnz; ++t) { out.col[t] = (int)ind[t]; out.val[t] = a->values[t]; }
+  } else {
+    // CSC of A -> CSR of A (counting sort by row).  The reference uploads the
+    // CSC arrays as the CSR of A^T and multiplies with the transpose flag
+    // (cusparse_wrapper.cpp:33-46,60-62); the product is the same A x.
+    std::vector<long long> cnt(n + 1, 0);
+    for (long long t = 0; t < nnz; ++t) cnt[ind[t] + 1]++;
+    for (long long i = 0; i < n; ++i) cnt[i + 1] += cnt[i];
+    out.ptr = cnt;
+    std::vector<long long> pos(cnt.begin(), cnt.end() - 1);
+    for (long long j = 0; j < n; ++j)
+      for (long long t = ptr[j]; t < ptr[j + 1]; ++t) {
+        const long long p = pos[ind[t]]++;
+        out.col[p] = (int)j;
+        out.val[p] = a->values[t];
+      }
+  }
+  e->nnz = nnz;
+  return GM_OK;
+}
+
+template <class VT>
+int upload_sell(gm_engine* e, const Csr& A, int sigma) {
+  const long long n = e->n;
+  const long long nsl = (n + 31) / 32;
+  std::vector<int> perm;  // slot -> row
+  bool sorted = sigma > 1;
+  std::vector<long long> rows(nsl * 32);
+  for (long long s = 0; s < nsl * 32; ++s) rows[s] = s < n ? s : -1;
+  if (sorted) {
+    for (long long w0 = 0; w0 < n; w0 += sigma) {
+      const long long w1 = std::min<long long>(n, w0 + sigma);
+      std::stable_sort(rows.begin() + w0, rows.begin() + w1, [&](long long x, long long y) {
+        return (A.ptr[x + 1] - A.ptr[x]) > (A.ptr[y + 1] - A.ptr[y]);
+      });
+    }
+  }
+  std::vector<long long> off(nsl + 1, 0);
+  for (long long s = 0; s < nsl; ++s) {
+    long long L = 0;
+    for (int l = 0; l < 32; ++l) {
+      const long long r = rows[s * 32 + l];
+      if (r >= 0) L = std::max(L, A.ptr[r + 1] - A.ptr[r]);
+    }
+    off[s + 1] = off[s] + 32 * L;
+  }
+  const long long padded = off[nsl];
+  if (padded > 2147483647LL * 2) return fail(e, GM_ERR_UNSUPPORTED, "padded SELL size too large");
+  std::vector<int> col(padded);
+  std::vector<VT> val(padded);
+  for (long long s = 0; s < nsl; ++s) {
+    const long long L = (off[s + 1] - off[s]) / 32;
+    for (int l = 0; l < 32; ++l) {
+      const long long r = rows[s * 32 + l];
+      const long long len = r >= 0 ? A.ptr[r + 1] - A.ptr[r] : 0;
+      for (long long jj = 0; jj < L; ++jj) {
+        const long long dst = off[s] + jj * 32 + l;
+        if (jj < len) {
+          col[dst] = A.col[A.ptr[r] + jj];
+          val[dst] = (VT)A.val[A.ptr[r] + jj];
+        } else {
+          col[dst] = r >= 0 ? (int)r : 0;
+          val[dst] = (VT)0;
+        }
+      }
+    }
+  }
+  long long* d_off;
+  int* d_col;
+  VT* d_val;
+  int rc;
+  if ((rc = dupload(e, &d_off, off.data(), off.size()))) return rc;
+  if ((rc = dupload(e, &d_col, col.data(), col.size()))) return rc;
+  if ((rc = dupload(e, &d_val, val.data(), val.size()))) return rc;
+  e->kp.slice_off = d_off;
+  e->kp.col = d_col;
+  e->kp.val = d_val;
+  e->kp.perm = nullptr;
+  if (sorted) {
+    std::vector<int> p32(rows.size());
+    for (size_t s = 0; s < rows.size(); ++s) p32[s] = (int)rows[s];
+    int* d_perm;
+    if ((rc = dupload(e, &d_perm, p32.data(), p32.size()))) return rc;
+    e->kp.perm = d_perm;
+  }
+  e->nslices = nsl;
+  e->padded = padded;
+  e->kp.nslices = nsl;
+  return GM_OK;
+}
+
+// Phase-group kernels (kern_fp64.cu / kern_mixed.cu): 0 lanczos, 1 solves,
+// 2 apply, 3 deflate/update, 4 fused lanczos + solves + apply.
+enum { KGRP_LANCZOS = 0, KGRP_SOLVE = 1, KGRP_APPLY = 2, KGRP_DEFLATE = 3, KGRP_FUSED = 4, KGRP_N = 5 };
+
+void* pick_kernel(int prec, int R, int group) {
+  return prec == GM_FP64 ? gm::kernel_fp64(R, group) : gm::kernel_mixed(R, group);
+}
+
+int group_of(int phases) {
+  const int solve = gm::PH_TRISOLVE | gm::PH_COEF;
+  const int defl = gm::PH_DEFLATE | gm::PH_UPDATE_FKPP | gm::PH_UPDATE_FHN;
+  if ((phases & gm::PH_LANCZOS) && (phases & (solve | gm::PH_APPLY))) return KGRP_FUSED;
+  if (phases & gm::PH_LANCZOS) return KGRP_LANCZOS;
+  if ((phases & solve) && (phases & gm::PH_APPLY)) return KGRP_FUSED;
+  if (phases & solve) return KGRP_SOLVE;
+  if (phases & gm::PH_APPLY) return KGRP_APPLY;
+  return KGRP_DEFLATE;
+}
+
+int map_status(gm_engine* e, int st) {
+  switch (st) {
+    case gm::ST_OK: return GM_OK;
+    case gm::ST_TIMEOUT: return fail(e, GM_ERR_TIMEOUT, "a grid-barrier wait exceeded its time limit; the handle is unusable");
+    case gm::ST_NONFINITE: return fail(e, GM_ERR_NONFINITE, "non-finite value in the Lanczos recurrence");
+    default: return fail(e, GM_ERR_CUDA, "device status %d", st);
+  }
+}
+
+int check_sync(gm_engine* e) {
+  GM_CUDA(e, cudaMemcpyAsync(e->h_status, e->kp.status, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+  GM_CUDA(e, cudaMemcpyAsync(e->h_status + 1, e->kp.meff, sizeof(int) * e->R, cudaMemcpyDeviceToHost, e->stream));
+  GM_CUDA(e, cudaStreamSynchronize(e->stream));
+  return map_status(e, e->h_status[0]);
+}
+
+// Launch the persistent kernel with the given phases; slot selects the event
+// pair used for gm_phase_times.
+int launch(gm_engine* e, int phases, int slot) {
+  GM_CUDA(e, cudaMemsetAsync(e->kp.bar, 0, sizeof(unsigned), e->stream));
+  KParams kp = e->kp;
+  kp.phases = phases;
+  void* args[] = {&kp};
+  GM_CUDA(e, cudaEventRecord(e->ev[slot][0], e->stream));
+  const int grp = group_of(phases);
+  kp.G = e->Gk[grp];
+  cudaError_t st = cudaLaunchCooperativeKernel(e->kfn[grp], dim3(kp.G), dim3(e->threads), args, 0, e->stream);
+  if (st != cudaSuccess) return cuda_fail(e, st, "cudaLaunchCooperativeKernel");
+  GM_CUDA(e, cudaEventRecord(e->ev[slot][1], e->stream));
+  e->ev_used[slot] = true;
+  e->launches++;
+  if (e->sync_mode) return check_sync(e);
+  return GM_OK;
+}
+
+int copy_out(gm_engine* e, const double* src_il, double* dst) {
+  if (!dst) return fail(e, GM_ERR_ARG, "null output pointer");
+  const long long total = e->n * e->R;
+  if (e->R == 1) {
+    GM_CUDA(e, cudaMemcpyAsync(dst, src_il, total * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+  } else {
+    k_pack_out<<<(unsigned)((total + 255) / 256), 256, 0, e->stream>>>(src_il, e->stage, e->n, e->R);
+    GM_CUDA(e, cudaGetLastError());
+    e->launches++;
+    GM_CUDA(e, cudaMemcpyAsync(dst, e->stage, total * sizeof(double), cudaMemcpyDeviceToHost, e->stream));
+  }
+  GM_CUDA(e, cudaStreamSynchronize(e->stream));
+  return GM_OK;
+}
+
+// Usol <- U (column-major n x R, host or device) scaled by col_scale.
+int set_usol(gm_engine* e, const double* U, bool on_device) {
+  if (!U) return fail(e, GM_ERR_ARG, "lanczos_create:badU: null U");
+  const long long total = e->n * e->R;
+  const double* src = U;
+  if (!on_device) {
+    GM_CUDA(e, cudaMemcpyAsync(e->stage, U, total * sizeof(double), cudaMemcpyHostToDevice, e->stream));
+    src = e->stage;
+  }
+  k_pack_in<<<(unsigned)((total + 255) / 256), 256, 0, e->stream>>>(src, e->kp.Usol, e->n, e->R, e->col_scale);
+  GM_CUDA(e, cudaGetLastError());
+  e->launches++;
+  return GM_OK;
+}
+
+void destroy(gm_engine* e) {
+  if (!e) return;
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  for (auto& b : e->bufs) cudaFree(b.p);
+  e->bufs.clear();
+  for (int s = 0; s < 5; ++s)
+    for (int t = 0; t < 2; ++t)
+      if (e->ev[s][t]) cudaEventDestroy(e->ev[s][t]);
+  if (e->h_status) cudaFreeHost(e->h_status);
+  if (e->own_stream) cudaStreamDestroy(e->own_stream);
+  delete e;
+}
+
+int create_impl(const gm_create_args* a, gm_engine* e) {
+  if (a->struct_version != GM_CREATE_ARGS_VERSION)
+    return fail(e, GM_ERR_ARG, "lanczos_create:invalidNumInputs: struct_version %d != %d", a->struct_version, GM_CREATE_ARGS_VERSION);
+  if (a->n <= 0) return fail(e, GM_ERR_ARG, "lanczos_create:inputNotSquare: n must be positive");
+  if (!a->ptr || (!a->ind && a->n > 0) || !a->values) return fail(e, GM_ERR_ARG, "lanczos_create:inputNotSparse: null sparse array");
+  if (a->format != GM_CSC && a->format != GM_CSR) return fail(e, GM_ERR_ARG, "unknown matrix format %d", a->format);
+  if (a->nrhs != 1 && a->nrhs != 2 && a->nrhs != 4) return fail(e, GM_ERR_ARG, "lanczos_create:badU: nrhs must be 1, 2 or 4 (got %d)", a->nrhs);
+  if (!a->U) return fail(e, GM_ERR_ARG, "lanczos_create:badU: null U");
+  if (a->num_eigs < 0 || (a->num_eigs > 0 && (!a->Q || !a->flam)))
+    return fail(e, GM_ERR_ARG, "lanczos_create:badQ: num_eigs %d needs Q and f(lambda)", a->num_eigs);
+  if (a->subspace_size < 1) return fail(e, GM_ERR_ARG, "lanczos_create:bad_N: subspace size must be >= 1");
+  if (a->gamma_size < 1 || !a->gamma) return fail(e, GM_ERR_ARG, "lanczos_create:bad_gamma: gamma_size must be >= 1");
+  if (a->contour_size < 1 || !a->gamma_s_real || !a->gamma_s_imag)
+    return fail(e, GM_ERR_ARG, "lanczos_create:bad_gamma_s_real: contour size must be >= 1");
+  if (!a->wts) return fail(e, GM_ERR_ARG, "lanczos_create:bad_wts1: null weights");
+  if (!a->shifts) return fail(e, GM_ERR_ARG, "lanczos_create:bad_shifts: null shifts");
+  if (a->precision != GM_FP64 && a->precision != GM_MIXED) return fail(e, GM_ERR_ARG, "unknown precision %d", a->precision);
+  if (a->n > 2147483647LL) return fail(e, GM_ERR_UNSUPPORTED, "n above 2^31-1");
+
+  e->n = a->n; e->R = a->nrhs; e->m = a->subspace_size; e->d = a->gamma_size - 1;
+  e->C = a->contour_size; e->k = a->num_eigs; e->prec = a->precision; e->sync_mode = a->sync_mode;
+  e->threads = a->threads_per_block ? a->threads_per_block : 512;
+  if (e->threads % 32 || e->threads < 64 || e->threads > 512)
+    return fail(e, GM_ERR_ARG, "threads_per_block must be a multiple of 32 in [64, 512]");
+  GM_CUDA(e, cudaGetDevice(&e->dev));
+  GM_CUDA(e, cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, e->dev));
+  int coop = 0;
+  GM_CUDA(e, cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, e->dev));
+  if (!coop) return fail(e, GM_ERR_UNSUPPORTED, "device does not support cooperative launch");
+  GM_CUDA(e, cudaStreamCreateWithFlags(&e->own_stream, cudaStreamNonBlocking));
+  e->stream = e->own_stream;
+  for (int s = 0; s < 5; ++s)
+    for (int t = 0; t < 2; ++t) GM_CUDA(e, cudaEventCreate(&e->ev[s][t]));
+  GM_CUDA(e, cudaHostAlloc((void**)&e->h_status, sizeof(int) * 8, cudaHostAllocDefault));
+
+  // Grid: blocks_per_sm x SMs, capped by co-residency of each phase-group
+  // kernel and by the work (at least ~4 SELL slices per warp: fewer blocks
+  // make every grid barrier cheaper on small problems).
+  const long long nsl = (e->n + 31) / 32;
+  const int nw = e->threads / 32;
+  const long long want = std::max<long long>(1, (nsl + 4LL * nw - 1) / (4LL * nw));
+  long long Gmax = 0;
+  for (int g = 0; g < KGRP_N; ++g) {
+    e->kfn[g] = pick_kernel(e->prec, e->R, g);
+    if (!e->kfn[g]) return fail(e, GM_ERR_UNSUPPORTED, "no kernel for nrhs %d", e->R);
+    int nb = 0;
+    GM_CUDA(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, e->kfn[g], e->threads, 0));
+    if (nb < 1) return fail(e, GM_ERR_UNSUPPORTED, "kernel group %d cannot be resident with %d threads", g, e->threads);
+    const int bps = a->blocks_per_sm > 0 ? std::min(a->blocks_per_sm, nb) : nb;
+    long long G = (long long)bps * e->nsm;
+    if (a->blocks_per_sm <= 0) G = std::min(G, want);
+    e->Gk[g] = (int)std::max<long long>(1, G);
+    Gmax = std::max(Gmax, (long long)e->Gk[g]);
+  }
+  e->G = (int)Gmax;
+
+  int rc;
+  Csr csr;
+  if ((rc = make_csr(e, a, csr))) return rc;
+  rc = e->prec == GM_FP64 ? upload_sell<double>(e, csr, a->sell_sigma) : upload_sell<float>(e, csr, a->sell_sigma);
+  if (rc) return rc;
+  csr = Csr();
+
+  KParams& kp = e->kp;
+  const long long n = e->n;
+  const int R = e->R, m = e->m, d = e->d, C = e->C, k = e->k;
+  kp.n = n; kp.m = m; kp.d = d; kp.C = C; kp.k = k; kp.G = e->G;
+  kp.dt = a->dt; kp.aode = a->aode; kp.bode = a->bode; kp.code = a->code; kp.vrest = a->vrest;
+  kp.vamp = a->vamp; kp.vpeak = a->vpeak; kp.c1ion = a->c1ion;
+  kp.bd_tol = a->breakdown_tol > 0 ? a->breakdown_tol : 64.0 * 2.220446049250313e-16;
+  const double tmo = a->barrier_timeout_s > 0 ? a->barrier_timeout_s : 5.0;
+  kp.timeout_ns = (unsigned long long)(tmo * 1e9);
+
+  double *gam, *gsr, *gsi, *wts, *shf, *flam = nullptr, *Q = nullptr, *mass, *ode;
+  if ((rc = dupload(e, &gam, a->gamma, d + 1))) return rc;
+  if ((rc = dupload(e, &gsr, a->gamma_s_real, (size_t)(d + 1) * C))) return rc;
+  if ((rc = dupload(e, &gsi, a->gamma_s_imag, (size_t)(d + 1) * C))) return rc;
+  if ((rc = dupload(e, &wts, a->wts, (size_t)2 * C * R))) return rc;
+  if ((rc = dupload(e, &shf, a->shifts, (size_t)2 * m * C * R))) return rc;
+  if (k > 0) {
+    if ((rc = dupload(e, &flam, a->flam, (size_t)k * R))) return rc;
+    if ((rc = dupload(e, &Q, a->Q, (size_t)k * n))) return rc;
+  }
+  std::vector<double> ones;
+  if (a->mass) {
+    if ((rc = dupload(e, &mass, a->mass, n))) return rc;
+  } else {
+    ones.assign(n, 1.0);
+    if ((rc = dupload(e, &mass, ones.data(), n))) return rc;
+  }
+  if (a->ode) {
+    if ((rc = dupload(e, &ode, a->ode, n))) return rc;
+  } else {
+    if ((rc = dalloc(e, &ode, n))) return rc;
+    GM_CUDA(e, cudaMemset(ode, 0, n * sizeof(double)));
+  }
+  std::vector<double> cs(R, 1.0);
+  if (a->col_scale) {
+    for (int r = 0; r < R; ++r) cs[r] = a->col_scale[r];
+  } else if (R == 2) {
+    cs[1] = a->dt;  // lanczos_impl.cu:79: U(:,1) *= dt
+  }
+  if ((rc = dupload(e, &e->col_scale, cs.data(), R))) return rc;
+  kp.gamma = gam; kp.gs_re = gsr; kp.gs_im = gsi; kp.wts = wts; kp.shifts = shf;
+  kp.flam = flam; kp.Q = Q; kp.mass = mass; kp.ode = ode;
+
+  const size_t nR = (size_t)n * R;
+  const size_t bsz = e->prec == GM_FP64 ? 8 : 4;
+  if ((rc = dalloc(e, &kp.U, nR))) return rc;
+  if ((rc = dalloc(e, &kp.Usol, nR))) return rc;
+  if ((rc = dalloc(e, &kp.upd, nR))) return rc;
+  if ((rc = dalloc(e, &kp.X, nR))) return rc;
+  if ((rc = dalloc(e, &kp.S, nR))) return rc;
+  if ((rc = dalloc(e, &e->stage, nR))) return rc;
+  char *V, *W0, *W1;
+  double *H0, *H1, *P;
+  if ((rc = dalloc(e, &V, (size_t)m * nR * bsz))) return rc;
+  if ((rc = dalloc(e, &W0, nR * bsz))) return rc;
+  if ((rc = dalloc(e, &W1, nR * bsz))) return rc;
+  if ((rc = dalloc(e, &H0, nR))) return rc;
+  if ((rc = dalloc(e, &H1, nR))) return rc;
+  if ((rc = dalloc(e, &P, d > 0 ? (size_t)(d + 1) * nR : 1))) return rc;
+  kp.V = V; kp.W0 = W0; kp.W1 = W1; kp.H0 = H0; kp.H1 = H1; kp.P = P;
+  if ((rc = dalloc(e, &kp.aabb, (size_t)(m + 1) * 2 * R))) return rc;
+  if ((rc = dalloc(e, &kp.Yr, (size_t)m * R * C))) return rc;
+  if ((rc = dalloc(e, &kp.Yi, (size_t)m * R * C))) return rc;
+  if ((rc = dalloc(e, &kp.coef, (size_t)R * (d + 1) * m))) return rc;
+  if ((rc = dalloc(e, &kp.coef_ff, (size_t)R * (d + 1) * m))) return rc;
+  if ((rc = dalloc(e, &kp.tri, (size_t)4 * m * R * C))) return rc;
+  if ((rc = dalloc(e, &kp.Z, (size_t)(k + 4) * R))) return rc;
+  if ((rc = dalloc(e, &kp.part, (size_t)(2 * R + (k + 4) * R) * e->G))) return rc;
+  if ((rc = dalloc(e, &kp.bar, 2))) return rc;
+  if ((rc = dalloc(e, &kp.status, 1))) return rc;
+  if ((rc = dalloc(e, &kp.meff, R))) return rc;
+  GM_CUDA(e, cudaMemset(kp.bar, 0, 2 * sizeof(unsigned)));
+  GM_CUDA(e, cudaMemset(kp.status, 0, sizeof(int)));
+  GM_CUDA(e, cudaMemset(kp.aabb, 0, (size_t)(m + 1) * 2 * R * sizeof(double)));
+  GM_CUDA(e, cudaMemset(kp.X, 0, nR * sizeof(double)));
+  GM_CUDA(e, cudaMemset(kp.Yr, 0, (size_t)m * R * C * sizeof(double)));
+  GM_CUDA(e, cudaMemset(kp.Yi, 0, (size_t)m * R * C * sizeof(double)));
+  {
+    std::vector<int> me(R, m);
+    GM_CUDA(e, cudaMemcpy(kp.meff, me.data(), R * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  GM_CUDA(e, cudaDeviceSynchronize());
+
+  // constructor: scale columns, Usol = U, deflate (lanczos_impl.cu:79-89)
+  if ((rc = set_usol(e, a->U, false))) return rc;
+  const int saved = e->sync_mode;
+  e->sync_mode = 1;
+  rc = launch(e, gm::PH_DEFLATE, 0);
+  e->sync_mode = saved;
+  return rc;
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+extern "C" {
+
+void gm_default_args(gm_create_args* a) {
+  if (!a) return;
+  std::memset(a, 0, sizeof(*a));
+  a->struct_version = GM_CREATE_ARGS_VERSION;
+  a->format = GM_CSC;
+  a->nrhs = 2;
+  a->sync_mode = 1;
+  a->dt = 1.0;
+  a->vamp = 1.0;
+}
+
+int gm_lanczos_create(const gm_create_args* args, gm_handle* out) {
+  g_create_error.clear();
+  if (!args || !out) return fail(nullptr, GM_ERR_ARG, "lanczos_create:invalidNumInputs: null argument");
+  *out = nullptr;
+  gm_engine* e = new (std::nothrow) gm_engine();
+  if (!e) return fail(nullptr, GM_ERR_OOM, "host allocation failed");
+  int rc = create_impl(args, e);
+  if (rc) {
+    g_create_error = e->err;
+    destroy(e);
+    return rc;
+  }
+  *out = e;
+  return GM_OK;
+}
+
+int gm_lanczos_delete(gm_handle h) {
+  if (!h) return fail(nullptr, GM_ERR_ARG, "lanczos_delete:inputNotHandle: null handle");
+  destroy(h);
+  return GM_OK;
+}
+
+int gm_build_subspace(gm_handle h) {
+  if (!h) return GM_ERR_ARG;
+  int rc = launch(h, gm::PH_LANCZOS, 1);
+  if (!rc) { h->have_V = true; h->have_y = false; h->have_coef = false; }
+  return rc;
+}
+
+int gm_lin_sys_solves(gm_handle h) {
+  if (!h) return GM_ERR_ARG;
+  if (!h->have_V) return fail(h, GM_ERR_STATE, "lin_sys_solves before build_subspace");
+  int rc = launch(h, gm::PH_TRISOLVE | gm::PH_COEF, 2);
+  if (!rc) { h->have_y = true; h->have_coef = true; }
+  return rc;
+}
+
+int gm_apply_V(gm_handle h) {
+  if (!h) return GM_ERR_ARG;
+  if (!h->have_V || !h->have_coef) return fail(h, GM_ERR_STATE, "apply_V before build_subspace and lin_sys_solves/set_y");
+  return launch(h, gm::PH_APPLY, 3);
+}
+
+int gm_update_U(gm_handle h) {
+  if (!h) return GM_ERR_ARG;
+  if (h->R != 2) return fail(h, GM_ERR_ARG, "update_U needs nrhs = 2");
+  return launch(h, gm::PH_UPDATE_FKPP | gm::PH_DEFLATE, 0);
+}
+
+int gm_update_U_monodomain(gm_handle h) {
+  if (!h) return GM_ERR_ARG;
+  if (h->R != 2) return fail(h, GM_ERR_ARG, "update_U_monodomain needs nrhs = 2");
+  return launch(h, gm::PH_UPDATE_FHN | gm::PH_DEFLATE, 0);
+}
+
+int gm_get_U(gm_handle h, double* dst) {
+  if (!h) return GM_ERR_ARG;
+  int rc = copy_out(h, h->kp.Usol, dst);
+  return rc ? rc : check_sync(h);
+}
+
+int gm_get_xsol(gm_handle h, double* dst) {
+  if (!h) return GM_ERR_ARG;
+  int rc = copy_out(h, h->kp.X, dst);
+  return rc ? rc : check_sync(h);
+}
+
+int gm_get_update(gm_handle h, double* dst) {
+  if (!h) return GM_ERR_ARG;
+  int rc = copy_out(h, h->kp.upd, dst);
+  return rc ? rc : check_sync(h);
+}
+
+int gm_get_solution(gm_handle h, double* dst) {
+  if (!h) return GM_ERR_ARG;
+  int rc = copy_out(h, h->kp.S, dst);
+  return rc ? rc : check_sync(h);
+}
+
+int gm_get_aabb(gm_handle h, double* dst) {
+  if (!h || !dst) return GM_ERR_ARG;
+  GM_CUDA(h, cudaMemcpyAsync(dst, h->kp.aabb, (size_t)(h->m + 1) * 2 * h->R * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return check_sync(h);
+}
+
+int gm_get_y(gm_handle h, double* yr, double* yi) {
+  if (!h) return GM_ERR_ARG;
+  const size_t cnt = (size_t)h->m * h->R * h->C;
+  if (yr) GM_CUDA(h, cudaMemcpyAsync(yr, h->kp.Yr, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  if (yi) GM_CUDA(h, cudaMemcpyAsync(yi, h->kp.Yi, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return check_sync(h);
+}
+
+int gm_set_y(gm_handle h, const double* yr, const double* yi) {
+  if (!h || !yr || !yi) return fail(h, GM_ERR_ARG, "set_y: null argument");
+  const size_t cnt = (size_t)h->m * h->R * h->C;
+  GM_CUDA(h, cudaMemcpyAsync(h->kp.Yr, yr, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  GM_CUDA(h, cudaMemcpyAsync(h->kp.Yi, yi, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  int rc = launch(h, gm::PH_COEF, 2);
+  if (!rc) { h->have_y = true; h->have_coef = true; }
+  return rc;
+}
+
+int gm_get_meff(gm_handle h, int* meff) {
+  if (!h || !meff) return GM_ERR_ARG;
+  int rc = check_sync(h);
+  for (int r = 0; r < h->R; ++r) meff[r] = h->h_status[1 + r];
+  return rc;
+}
+
+static int set_U_common(gm_handle h, const double* U, bool on_device) {
+  if (!h) return GM_ERR_ARG;
+  int rc = set_usol(h, U, on_device);
+  if (rc) return rc;
+  GM_CUDA(h, cudaMemsetAsync(h->kp.status, 0, sizeof(int), h->stream));
+  h->have_V = h->have_y = h->have_coef = false;
+  return launch(h, gm::PH_DEFLATE, 0);
+}
+
+int gm_set_U(gm_handle h, const double* U_host) { return set_U_common(h, U_host, false); }
+
+int gm_set_U_device(gm_handle h, const double* U_dev) { return set_U_common(h, U_dev, true); }
+
+int gm_solve(gm_handle h) {
+  if (!h) return GM_ERR_ARG;
+  int rc = launch(h, gm::PH_LANCZOS | gm::PH_TRISOLVE | gm::PH_COEF | gm::PH_APPLY | gm::PH_APPLY_SET, 4);
+  if (!rc) h->have_V = h->have_y = h->have_coef = true;
+  return rc;
+}
+
+int gm_solve_host(gm_handle h, const double* b_host, double* x_host) {
+  if (!h) return GM_ERR_ARG;
+  int rc = gm_set_U(h, b_host);
+  if (rc) return rc;
+  rc = gm_solve(h);
+  if (rc) return rc;
+  return gm_get_solution(h, x_host);
+}
+
+int gm_sync(gm_handle h) {
+  if (!h) return GM_ERR_ARG;
+  return check_sync(h);
+}
+
+int gm_set_stream(gm_handle h, void* stream) {
+  if (!h) return GM_ERR_ARG;
+  GM_CUDA(h, cudaStreamSynchronize(h->stream));
+  h->stream = stream ? reinterpret_cast<cudaStream_t>(stream) : h->own_stream;
+  return GM_OK;
+}
+
+int gm_phase_times(gm_handle h, float* ms) {
+  if (!h || !ms) return GM_ERR_ARG;
+  GM_CUDA(h, cudaStreamSynchronize(h->stream));
+  for (int s = 0; s < 5; ++s) {
+    ms[s] = 0.f;
+    if (h->ev_used[s]) GM_CUDA(h, cudaEventElapsedTime(&ms[s], h->ev[s][0], h->ev[s][1]));
+  }
+  return GM_OK;
+}
+
+int gm_info(gm_handle h, int64_t* info) {
+  if (!h || !info) return GM_ERR_ARG;
+  info[0] = h->n; info[1] = h->R; info[2] = h->m; info[3] = h->d; info[4] = h->C; info[5] = h->k;
+  info[6] = h->prec; info[7] = h->G; info[8] = h->threads; info[9] = h->padded;
+  info[10] = (int64_t)h->bytes; info[11] = h->launches;
+  return GM_OK;
+}
+
+const char* gm_last_error(gm_handle h) {
+  return h ? h->err.c_str() : g_create_error.c_str();
+}
+
+const char* gm_version(void) { return "gpumatfun-gb300 0.1.0 (sm_103a)"; }
+
+}  // extern "C"

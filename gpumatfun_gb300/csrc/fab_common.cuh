@@ -1,0 +1,314 @@
+// Common device layer of the f(A)b engine: status codes, float-float
+// arithmetic, precision policies, vector loads, a bounded grid barrier and
+// deterministic block/grid reductions.
+//
+// Precision policies
+//   PolFP64  : matrix values, Krylov basis and work vectors in FP64, every
+//              per-element operation in FP64 (the plain engine).
+//   PolMixed : matrix values, Krylov basis V and Lanczos work vector W in FP32;
+//              Horner and lift buffers as float-float pairs; every per-element
+//              operation on the FP32 pipe with exact products (two_prod) and
+//              compensated sums (float-float, ~48-bit significand).  FP64 is
+//              used only for per-thread reduction totals and the scalar
+//              recurrences (alpha, beta, tridiagonal solves, quadrature sum).
+//              On GB300 the FP64 rate is ~1/64 of FP32, so this keeps the
+//              mixed engine HBM-bound instead of FP64-bound.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gm {
+
+enum Status : int {
+  ST_OK = 0, ST_ARG = 1, ST_OOM = 2, ST_CUDA = 3, ST_BREAKDOWN = 4,
+  ST_TIMEOUT = 5, ST_STATE = 6, ST_NONFINITE = 7, ST_UNSUPPORTED = 8
+};
+
+// ---------------------------------------------------------------- float-float
+struct ff { float hi, lo; };
+
+__device__ __forceinline__ ff two_sum(float a, float b) {
+  float s = a + b;
+  float bb = s - a;
+  float e = (a - (s - bb)) + (b - bb);
+  return {s, e};
+}
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {  // |a| >= |b|
+  float s = a + b;
+  float e = b - (s - a);
+  return {s, e};
+}
+__device__ __forceinline__ ff two_prod(float a, float b) {
+  float p = a * b;
+  float e = fmaf(a, b, -p);
+  return {p, e};
+}
+__device__ __forceinline__ ff ff_add(ff a, ff b) {
+  ff s = two_sum(a.hi, b.hi);
+  float e = s.lo + (a.lo + b.lo);
+  return fast_two_sum(s.hi, e);
+}
+__device__ __forceinline__ ff ff_neg(ff a) { return {-a.hi, -a.lo}; }
+// a * b with b a single float
+__device__ __forceinline__ ff ff_mulf(ff a, float b) {
+  ff p = two_prod(a.hi, b);
+  p.lo = fmaf(a.lo, b, p.lo);
+  return fast_two_sum(p.hi, p.lo);
+}
+__device__ __forceinline__ ff ff_mul(ff a, ff b) {
+  ff p = two_prod(a.hi, b.hi);
+  p.lo = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo));
+  return fast_two_sum(p.hi, p.lo);
+}
+// acc + a*b, a and b floats (exact product, compensated sum)
+__device__ __forceinline__ ff ff_fma_ff(ff acc, float a, float b) {
+  ff p = two_prod(a, b);
+  ff s = two_sum(acc.hi, p.hi);
+  float e = s.lo + (acc.lo + p.lo);
+  return fast_two_sum(s.hi, e);
+}
+__device__ __forceinline__ ff ff_from_double(double x) {
+  float h = (float)x;
+  float l = (float)(x - (double)h);
+  return {h, l};
+}
+__device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
+
+// ---------------------------------------------------------------- policies
+struct PolFP64 {
+  using VT = double;   // matrix values
+  using BT = double;   // Krylov basis V and Lanczos work vector W
+  using HT = double;   // Horner / lift buffers
+  using AT = double;   // per-element accumulator
+  using ST = double;   // scalar used in per-element operations
+  static constexpr bool kMixed = false;
+  __device__ static __forceinline__ AT zero() { return 0.0; }
+  __device__ static __forceinline__ ST scalar(double s) { return s; }
+  __device__ static __forceinline__ AT acc(AT a, VT v, double x) { return fma(v, x, a); }
+  __device__ static __forceinline__ AT mul(AT z, ST s) { return z * s; }
+  __device__ static __forceinline__ AT add_mul(AT w, ST s, double v) { return fma(s, v, w); }
+  __device__ static __forceinline__ AT sub_mul(AT w, ST s, double v) { return fma(-s, v, w); }
+  __device__ static __forceinline__ AT add(AT a, AT b) { return a + b; }
+  __device__ static __forceinline__ AT dot(AT a, AT w, double v) { return fma(w, v, a); }
+  __device__ static __forceinline__ AT dot_self(AT a, AT w) { return fma(w, w, a); }
+  __device__ static __forceinline__ double to_d(AT a) { return a; }
+  __device__ static __forceinline__ AT from_d(double a) { return a; }
+  __device__ static __forceinline__ BT to_b(AT a) { return a; }
+  __device__ static __forceinline__ HT to_h(AT a) { return a; }
+  __device__ static __forceinline__ AT from_b(BT b) { return b; }
+  // b * s rounded to storage: v = w * rbeta
+  __device__ static __forceinline__ BT scale_to_b(BT b, ST s) { return b * s; }
+};
+
+struct PolMixed {
+  using VT = float;
+  using BT = float;
+  using HT = float2;   // float-float pair (x = hi, y = lo)
+  using AT = ff;
+  using ST = ff;
+  static constexpr bool kMixed = true;
+  __device__ static __forceinline__ AT zero() { return {0.f, 0.f}; }
+  __device__ static __forceinline__ ST scalar(double s) { return ff_from_double(s); }
+  __device__ static __forceinline__ AT acc(AT a, VT v, float x) { return ff_fma_ff(a, v, x); }
+  __device__ static __forceinline__ AT acc(AT a, VT v, float2 x) {
+    // v * (x.hi + x.lo): exact v*x.hi plus the small v*x.lo term
+    ff p = two_prod(v, x.x);
+    p.lo = fmaf(v, x.y, p.lo);
+    ff s = two_sum(a.hi, p.hi);
+    float e = s.lo + (a.lo + p.lo);
+    return fast_two_sum(s.hi, e);
+  }
+  __device__ static __forceinline__ AT mul(AT z, ST s) { return ff_mul(z, s); }
+  __device__ static __forceinline__ AT add_mul(AT w, ST s, float v) { return ff_add(w, ff_mulf(s, v)); }
+  __device__ static __forceinline__ AT sub_mul(AT w, ST s, float v) { return ff_add(w, ff_neg(ff_mulf(s, v))); }
+  __device__ static __forceinline__ AT add(AT a, AT b) { return ff_add(a, b); }
+  __device__ static __forceinline__ AT dot(AT a, AT w, float v) { return ff_add(a, ff_mulf(w, v)); }
+  __device__ static __forceinline__ AT dot_self(AT a, AT w) { return ff_add(a, ff_mul(w, w)); }
+  __device__ static __forceinline__ double to_d(AT a) { return ff_to_double(a); }
+  __device__ static __forceinline__ AT from_d(double a) { return ff_from_double(a); }
+  __device__ static __forceinline__ BT to_b(AT a) { return a.hi + a.lo; }
+  __device__ static __forceinline__ HT to_h(AT a) { return make_float2(a.hi, a.lo); }
+  __device__ static __forceinline__ AT from_b(BT b) { return {b, 0.f}; }
+  __device__ static __forceinline__ AT from_h(HT h) { return {h.x, h.y}; }
+  __device__ static __forceinline__ BT scale_to_b(BT b, ST s) {
+    ff p = ff_mulf(s, b);
+    return p.hi + p.lo;
+  }
+};
+
+__device__ __forceinline__ double h_to_d(double h) { return h; }
+__device__ __forceinline__ double h_to_d(float2 h) { return (double)h.x + (double)h.y; }
+__device__ __forceinline__ float2 h_from_ff(ff a) { return make_float2(a.hi, a.lo); }
+
+// ---------------------------------------------------------------- vector I/O
+// R consecutive values (one row of an interleaved [n][R] vector).
+template <int R> struct VecIO;
+template <> struct VecIO<1> {
+  template <class T> __device__ static __forceinline__ void ld(const T* p, T (&o)[1]) { o[0] = p[0]; }
+  template <class T> __device__ static __forceinline__ void st(T* p, const T (&o)[1]) { p[0] = o[0]; }
+};
+template <> struct VecIO<2> {
+  __device__ static __forceinline__ void ld(const double* p, double (&o)[2]) {
+    double2 v = *reinterpret_cast<const double2*>(p); o[0] = v.x; o[1] = v.y;
+  }
+  __device__ static __forceinline__ void st(double* p, const double (&o)[2]) {
+    *reinterpret_cast<double2*>(p) = make_double2(o[0], o[1]);
+  }
+  __device__ static __forceinline__ void ld(const float* p, float (&o)[2]) {
+    float2 v = *reinterpret_cast<const float2*>(p); o[0] = v.x; o[1] = v.y;
+  }
+  __device__ static __forceinline__ void st(float* p, const float (&o)[2]) {
+    *reinterpret_cast<float2*>(p) = make_float2(o[0], o[1]);
+  }
+  __device__ static __forceinline__ void ld(const float2* p, float2 (&o)[2]) {
+    float4 v = *reinterpret_cast<const float4*>(p); o[0] = make_float2(v.x, v.y); o[1] = make_float2(v.z, v.w);
+  }
+  __device__ static __forceinline__ void st(float2* p, const float2 (&o)[2]) {
+    *reinterpret_cast<float4*>(p) = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
+  }
+};
+template <> struct VecIO<4> {
+  __device__ static __forceinline__ void ld(const double* p, double (&o)[4]) {
+    double2 a = reinterpret_cast<const double2*>(p)[0];
+    double2 b = reinterpret_cast<const double2*>(p)[1];
+    o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y;
+  }
+  __device__ static __forceinline__ void st(double* p, const double (&o)[4]) {
+    reinterpret_cast<double2*>(p)[0] = make_double2(o[0], o[1]);
+    reinterpret_cast<double2*>(p)[1] = make_double2(o[2], o[3]);
+  }
+  __device__ static __forceinline__ void ld(const float* p, float (&o)[4]) {
+    float4 v = *reinterpret_cast<const float4*>(p); o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w;
+  }
+  __device__ static __forceinline__ void st(float* p, const float (&o)[4]) {
+    *reinterpret_cast<float4*>(p) = make_float4(o[0], o[1], o[2], o[3]);
+  }
+  __device__ static __forceinline__ void ld(const float2* p, float2 (&o)[4]) {
+    float4 a = reinterpret_cast<const float4*>(p)[0];
+    float4 b = reinterpret_cast<const float4*>(p)[1];
+    o[0] = make_float2(a.x, a.y); o[1] = make_float2(a.z, a.w);
+    o[2] = make_float2(b.x, b.y); o[3] = make_float2(b.z, b.w);
+  }
+  __device__ static __forceinline__ void st(float2* p, const float2 (&o)[4]) {
+    reinterpret_cast<float4*>(p)[0] = make_float4(o[0].x, o[0].y, o[1].x, o[1].y);
+    reinterpret_cast<float4*>(p)[1] = make_float4(o[2].x, o[2].y, o[3].x, o[3].y);
+  }
+};
+
+// ---------------------------------------------------------------- grid barrier
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+  asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long global_timer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Sense-by-generation barrier over a group of co-resident blocks.  Every wait
+// is bounded: after timeout_ns the waiting block records ST_TIMEOUT in *status
+// and all blocks leave at their next barrier.  Returns false when the kernel
+// must stop (timeout or an error recorded by any block).
+struct GridBar {
+  unsigned* count;
+  unsigned* gen;
+  int* status;
+  unsigned nblocks;
+  unsigned long long timeout_ns;
+
+  __device__ bool sync() const {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int ok = 1;
+      if (nblocks > 1) {
+        unsigned g = ld_acquire_u32(gen);
+        __threadfence();
+        unsigned prev = atomicAdd(count, 1u);
+        if (prev == nblocks - 1) {
+          atomicExch(count, 0u);
+          __threadfence();
+          st_release_u32(gen, g + 1u);
+        } else {
+          unsigned long long t0 = global_timer_ns();
+          unsigned spins = 0;
+          while (ld_acquire_u32(gen) == g) {
+            if ((++spins & 31u) == 0u) {
+              if (*(volatile int*)status != 0) { ok = 0; break; }
+              if (global_timer_ns() - t0 > timeout_ns) {
+                atomicCAS(status, 0, (int)ST_TIMEOUT);
+                ok = 0;
+                break;
+              }
+            }
+            __nanosleep(32);
+          }
+        }
+        __threadfence();
+      }
+      if (*(volatile int*)status != 0) ok = 0;
+      s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+  }
+};
+
+// ---------------------------------------------------------------- reductions
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-sum of N values per thread; thread 0 writes out[j * stride] for j < N.
+// Fixed reduction tree, so the result does not depend on timing.
+template <int N>
+__device__ __forceinline__ void block_sum_store(double (&v)[N], double* out, long long stride) {
+  __shared__ double red[32][N > 0 ? N : 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int j = 0; j < N; ++j) v[j] = warp_sum(v[j]);
+  if (lane == 0) {
+#pragma unroll
+    for (int j = 0; j < N; ++j) red[warp][j] = v[j];
+  }
+  __syncthreads();
+  if (warp == 0) {
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      double t = lane < nw ? red[lane][j] : 0.0;
+      t = warp_sum(t);
+      if (lane == 0) out[j * stride] = t;
+    }
+  }
+  __syncthreads();
+}
+
+// Every block computes the same total of G per-block partials for N
+// quantities (partials laid out [N][G]); deterministic fixed order.
+template <int N>
+__device__ __forceinline__ void grid_total(const double* partials, int G, double (&tot)[N]) {
+  __shared__ double s_tot[N > 0 ? N : 1];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp == 0) {
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      double t = 0.0;
+      for (int b = lane; b < G; b += 32) t += partials[(long long)j * G + b];
+      t = warp_sum(t);
+      if (lane == 0) s_tot[j] = t;
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int j = 0; j < N; ++j) tot[j] = s_tot[j];
+  __syncthreads();
+}
+
+}  // namespace gm

@@ -1,0 +1,216 @@
+/*
+ * gpumatfun.h -- C ABI of the GB300-native f(A)b engine.
+ *
+ * The engine computes f(A) b for a sparse symmetric A by polynomial-
+ * preconditioned Lanczos, deflation by k known eigenvectors and the
+ * Hale-Higham-Trefethen contour integral evaluated through batched shifted
+ * complex tridiagonal solves.  Each entry point below replaces one MEX
+ * gateway of the reference (GPUMatfun, MATLAB -> MEX -> CUDA) and keeps its
+ * meaning; the MEX shim in gpumatfun_gb300/mex/ maps the MATLAB arguments
+ * onto these calls.
+ *
+ * Conventions
+ *  - Host arrays are column-major, as MATLAB stores them.
+ *  - Every function returns a gm_status; GM_OK is 0.  On failure the
+ *    message is available from gm_last_error(h) (or gm_last_error(NULL)
+ *    for failures before a handle exists).
+ *  - A handle owns all its device memory and one CUDA stream.  A handle is
+ *    not thread-safe; different handles may be used from different threads.
+ *  - With sync_mode = 1 (default) each call waits for its kernels and
+ *    checks the device status word; with sync_mode = 0 calls are
+ *    asynchronous on the handle's stream until gm_sync or a gm_get_* call.
+ */
+#ifndef GPUMATFUN_H
+#define GPUMATFUN_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GM_CREATE_ARGS_VERSION 1
+
+typedef struct gm_engine* gm_handle;
+
+typedef enum gm_status {
+  GM_OK = 0,
+  GM_ERR_ARG = 1,          /* invalid argument (shape, size, pointer)           */
+  GM_ERR_OOM = 2,          /* device allocation failed                          */
+  GM_ERR_CUDA = 3,         /* CUDA runtime error                                */
+  GM_ERR_BREAKDOWN = 4,    /* Lanczos breakdown in every right-hand side        */
+  GM_ERR_TIMEOUT = 5,      /* a bounded grid-barrier wait expired               */
+  GM_ERR_STATE = 6,        /* call out of order (e.g. apply before solves)      */
+  GM_ERR_NONFINITE = 7,    /* NaN/Inf met in the recurrence                     */
+  GM_ERR_UNSUPPORTED = 8   /* option not available on this device/build         */
+} gm_status;
+
+typedef enum gm_precision {
+  GM_FP64 = 0,   /* FP64 values, basis and arithmetic (the reference's precision) */
+  GM_MIXED = 1   /* FP32 values and Krylov basis; exact products and compensated
+                    sums on the FP32 pipe; FP64 alpha/beta recurrence, tridiagonal
+                    solves and quadrature */
+} gm_precision;
+
+typedef enum gm_matrix_format {
+  GM_CSC = 0,    /* MATLAB sparse storage: colptr (jc), rowind (ir), values (pr) */
+  GM_CSR = 1
+} gm_matrix_format;
+
+/* Arguments of gm_lanczos_create.  The first block carries exactly the 26
+ * positional arguments of lanczos_create (lanczos_create.cpp:7-32,
+ * lanczosEngine.m:9); nrhs generalises the reference's fixed pair of
+ * right-hand sides (column 0 = exp part with wts1/exp_lambda, column 1 = phi
+ * part with wts2/phi_lambda). */
+typedef struct gm_create_args {
+  int struct_version;          /* GM_CREATE_ARGS_VERSION                         */
+  /* A: n x n sparse (lanczos_create.cpp:69-118) */
+  int64_t n;
+  int64_t nnz;                 /* stored entries; taken as colptr[n] when 0      */
+  int format;                  /* gm_matrix_format                               */
+  const int64_t* ptr;          /* n+1 column (CSC) or row (CSR) pointers          */
+  const int64_t* ind;          /* nnz row (CSC) or column (CSR) indices           */
+  const double* values;        /* nnz                                             */
+  /* U: n x nrhs right-hand sides (ARG_U) */
+  int nrhs;
+  const double* U;
+  /* deflation: Q n x k, lambda k (unused on device, as in the reference),
+   * flam k x nrhs = f_r(lambda) (exp_lambda / phi_lambda for the reference) */
+  int num_eigs;
+  const double* Q;
+  const double* lambda;
+  const double* flam;
+  /* Krylov dimension (ARG_N) and polynomial preconditioner (ARG_gamma) */
+  int subspace_size;
+  int gamma_size;              /* d + 1 */
+  const double* gamma;
+  /* contour: gamma_s_{real,imag} (d+1) x C; wts: nrhs blocks of C x 2
+   * [re, im] (wts1, wts2); shifts: 2*m*C*nrhs (the reference's 4mC) */
+  int contour_size;
+  const double* gamma_s_real;
+  const double* gamma_s_imag;
+  const double* wts;
+  const double* shifts;
+  /* time stepping (ARG_dt, ARG_ode .. ARG_c2ion, ARG_mass) */
+  double dt;
+  const double* col_scale;     /* nrhs; NULL = reference convention [1, dt]     */
+  const double* mass;          /* n; NULL = ones                                  */
+  const double* ode;           /* n; NULL = zeros                                 */
+  double aode, bode, code, vrest, vamp, vth, vpeak, c1ion, c2ion;
+  /* engine options (no counterpart in the reference) */
+  int precision;               /* gm_precision                                    */
+  int sync_mode;               /* 1 = synchronous checked calls (default)        */
+  int threads_per_block;       /* 0 = 512                                         */
+  int blocks_per_sm;           /* 0 = occupancy-limited, at most 2                */
+  int sell_sigma;              /* SELL-32 sorting window in rows; 0/1 = unsorted  */
+  double barrier_timeout_s;    /* 0 = 5 s                                         */
+  double breakdown_tol;        /* 0 = 64 eps, relative to |alpha_j| + beta_j      */
+} gm_create_args;
+
+/* Fill *args with defaults (zeros, struct_version, sync_mode = 1, nrhs = 2). */
+void gm_default_args(gm_create_args* args);
+
+/* Replaces lanczos_create (lanczos_create.cpp:35-766 and the engine
+ * constructor lanczos_impl.cu:5-91): uploads A, Q, U and the method
+ * parameters, scales U's columns by col_scale, keeps Usol = U and deflates:
+ * Z = Q^T U, U <- U - Q Z, update = Q (f(lambda) o Z). */
+int gm_lanczos_create(const gm_create_args* args, gm_handle* out);
+
+/* Replaces lanczos_delete (lanczos_delete.cpp:6-35). */
+int gm_lanczos_delete(gm_handle h);
+
+/* Replaces build_subspace_mex (build_subspace.cpp:6-35, build_subspace.cu:5-91):
+ * m steps of Lanczos on A p(A) for every right-hand side; fills V and aabb. */
+int gm_build_subspace(gm_handle h);
+
+/* Replaces lin_sys_solves_mex (lin_sys_solves.cpp:6-35, lin_sys_solves.cu:5-21):
+ * y_{r,j} = w_{r,j} beta0_r (sigma_j I - T_r)^{-1} e1 for every node and RHS. */
+int gm_lin_sys_solves(gm_handle h);
+
+/* Replaces apply_V_mex (apply_V.cpp:6-35, apply_V.cu:5-95):
+ * X_r += sum_j Im(q_j(A) V_r y_{r,j}). */
+int gm_apply_V(gm_handle h);
+
+/* Replaces update_U_mex (update_U.cpp:6-35, update_U.cu:5-32): Fisher-KPP
+ * exponential-Euler step, re-deflation, X = 0.  Needs nrhs = 2. */
+int gm_update_U(gm_handle h);
+
+/* Replaces update_U_monodomain_mex (update_U_monodomain.cpp:6-35,
+ * update_U_monodomain.cu:5-43): FitzHugh-Nagumo step. Needs nrhs = 2. */
+int gm_update_U_monodomain(gm_handle h);
+
+/* Replaces get_U_mex (get_U.cpp:6-38, lanczos_impl.cu:502-506): copies Usol
+ * (n x nrhs, column-major) to dst. */
+int gm_get_U(gm_handle h, double* dst);
+
+/* Replaces get_xsol_mex (get_xsol.cpp:6-38, lanczos_impl.cu:508-512): copies
+ * X (n x nrhs, column-major) to dst. */
+int gm_get_xsol(gm_handle h, double* dst);
+
+/* Implements lanczosEngine.get_aabb (lanczosEngine.m:25-27), whose MEX file
+ * the reference never shipped: copies aabb ((m+1) x 2*nrhs, alpha columns then
+ * beta columns) to dst. */
+int gm_get_aabb(gm_handle h, double* dst);
+
+/* Implements lanczosEngine.set_y (lanczosEngine.m:29-31), whose MEX file the
+ * reference never shipped: sets Yreal/Yimag (m x nrhs*C) for apply_V. */
+int gm_set_y(gm_handle h, const double* yreal, const double* yimag);
+
+/* Copies Yreal and Yimag (m x nrhs*C each) to the host (either may be NULL). */
+int gm_get_y(gm_handle h, double* yreal, double* yimag);
+
+/* ---- additions with no reference counterpart ------------------------------ */
+
+/* New right-hand sides (n x nrhs, column-major, host): U <- U_host o col_scale,
+ * Usol = U, re-deflate, X = 0. */
+int gm_set_U(gm_handle h, const double* U_host);
+
+/* As gm_set_U with U a device pointer (column-major n x nrhs) on the
+ * handle's device; asynchronous on the handle's stream. */
+int gm_set_U_device(gm_handle h, const double* U_dev);
+
+/* Copies the deflation update Q (f(lambda) o Q^T U) (n x nrhs) to dst. */
+int gm_get_update(gm_handle h, double* dst);
+
+/* f(A) b for every column: X + update (n x nrhs, column-major) to dst. */
+int gm_get_solution(gm_handle h, double* dst);
+
+/* One f(A)b evaluation in a single persistent launch: build_subspace,
+ * lin_sys_solves and apply_V fused; then X + update is available. */
+int gm_solve(gm_handle h);
+
+/* End to end with host buffers: set_U(b_host), gm_solve, solution -> x_host. */
+int gm_solve_host(gm_handle h, const double* b_host, double* x_host);
+
+/* Waits for the handle's stream and returns the device status. */
+int gm_sync(gm_handle h);
+
+/* Uses an external CUDA stream (cudaStream_t passed as void*); NULL restores
+ * the handle's own stream. */
+int gm_set_stream(gm_handle h, void* stream);
+
+/* Device milliseconds of the last launch of each phase group, measured with
+ * CUDA events on the handle's stream: [0] deflate/update, [1] build_subspace,
+ * [2] lin_sys_solves, [3] apply_V, [4] fused solve. */
+int gm_phase_times(gm_handle h, float* ms5);
+
+/* Engine facts: [0] n, [1] nrhs, [2] m, [3] d, [4] C, [5] k, [6] precision,
+ * [7] grid blocks, [8] threads per block, [9] SELL padded entries,
+ * [10] device bytes held, [11] kernel launches so far. */
+int gm_info(gm_handle h, int64_t* info12);
+
+/* Effective Krylov dimension per RHS after the last build (< m after a
+ * breakdown). */
+int gm_get_meff(gm_handle h, int* meff);
+
+/* Last error message of h (or of the last failed create when h is NULL). */
+const char* gm_last_error(gm_handle h);
+
+/* Library version string. */
+const char* gm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPUMATFUN_H */
