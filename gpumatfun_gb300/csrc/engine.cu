@@ -41,6 +41,7 @@ struct gm_engine {
   long long n = 0, nnz = 0, nslices = 0, padded = 0;
   int R = 0, m = 0, d = 0, C = 0, k = 0, prec = 0, sync_mode = 1;
   int threads = 512, G = 0;
+  int scale_exp = 0;             // mixed engine: A stored as A * 2^-scale_exp
   int Gk[5] = {};                // grid size per phase group (co-residency bound)
   void* kfn[5] = {};
   std::vector<DevBuf> bufs;
@@ -165,7 +166,7 @@ int make_csr(gm_engine* e, const gm_create_args* a, Csr& out) {
 }
 
 template <class VT>
-int upload_sell(gm_engine* e, const Csr& A, int sigma) {
+int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp) {
   const long long n = e->n;
   const long long nsl = (n + 31) / 32;
   std::vector<int> perm;  // slot -> row
@@ -202,7 +203,7 @@ int upload_sell(gm_engine* e, const Csr& A, int sigma) {
         const long long dst = off[s] + jj * 32 + l;
         if (jj < len) {
           col[dst] = A.col[A.ptr[r] + jj];
-          val[dst] = (VT)A.val[A.ptr[r] + jj];
+          val[dst] = (VT)std::ldexp(A.val[A.ptr[r] + jj], -scale_exp);
         } else {
           col[dst] = r >= 0 ? (int)r : 0;
           val[dst] = (VT)0;
@@ -272,7 +273,8 @@ int check_sync(gm_engine* e) {
 // Launch the persistent kernel with the given phases; slot selects the event
 // pair used for gm_phase_times.
 int launch(gm_engine* e, int phases, int slot) {
-  GM_CUDA(e, cudaMemsetAsync(e->kp.bar, 0, sizeof(unsigned), e->stream));
+  // The barrier counter returns to 0 after every completed barrier; it is
+  // reset explicitly only after an aborted launch (gm_set_U clears errors).
   KParams kp = e->kp;
   kp.phases = phases;
   void* args[] = {&kp};
@@ -367,11 +369,11 @@ int create_impl(const gm_create_args* a, gm_engine* e) {
   GM_CUDA(e, cudaHostAlloc((void**)&e->h_status, sizeof(int) * 8, cudaHostAllocDefault));
 
   // Grid: blocks_per_sm x SMs, capped by co-residency of each phase-group
-  // kernel and by the work (at least ~4 SELL slices per warp: fewer blocks
-  // make every grid barrier cheaper on small problems).
+  // kernel and by the work (about one SELL slice per warp: small problems
+  // get fewer blocks, which makes every grid barrier cheaper).
   const long long nsl = (e->n + 31) / 32;
   const int nw = e->threads / 32;
-  const long long want = std::max<long long>(1, (nsl + 4LL * nw - 1) / (4LL * nw));
+  const long long want = std::max<long long>(1, (nsl + nw - 1) / nw);
   long long Gmax = 0;
   for (int g = 0; g < KGRP_N; ++g) {
     e->kfn[g] = pick_kernel(e->prec, e->R, g);
@@ -390,7 +392,23 @@ int create_impl(const gm_create_args* a, gm_engine* e) {
   int rc;
   Csr csr;
   if ((rc = make_csr(e, a, csr))) return rc;
-  rc = e->prec == GM_FP64 ? upload_sell<double>(e, csr, a->sell_sigma) : upload_sell<float>(e, csr, a->sell_sigma);
+  // The mixed engine stores A / 2^e (e = floor(log2 of the largest absolute
+  // row sum)) so that A's spectrum, the polynomial coefficients and the
+  // Horner intermediates stay inside FP32's exponent range.  The scaling is a
+  // power of two, hence exact, and is undone exactly: gamma_i, the shifted
+  // coefficients, the shifts and the weights are rescaled so that y and X
+  // are unchanged (sigma/s - T/s = (sigma - T)/s, A_s^(d-i) s^(d-i) = A^(d-i)).
+  if (e->prec == GM_MIXED) {
+    double mx = 0.0;
+    for (long long i = 0; i < e->n; ++i) {
+      double rs = 0.0;
+      for (long long t = csr.ptr[i]; t < csr.ptr[i + 1]; ++t) rs += std::fabs(csr.val[t]);
+      mx = std::max(mx, rs);
+    }
+    e->scale_exp = mx > 0.0 ? (int)std::floor(std::log2(mx)) : 0;
+  }
+  rc = e->prec == GM_FP64 ? upload_sell<double>(e, csr, a->sell_sigma, 0)
+                          : upload_sell<float>(e, csr, a->sell_sigma, e->scale_exp);
   if (rc) return rc;
   csr = Csr();
 
@@ -405,11 +423,30 @@ int create_impl(const gm_create_args* a, gm_engine* e) {
   kp.timeout_ns = (unsigned long long)(tmo * 1e9);
 
   double *gam, *gsr, *gsi, *wts, *shf, *flam = nullptr, *Q = nullptr, *mass, *ode;
-  if ((rc = dupload(e, &gam, a->gamma, d + 1))) return rc;
-  if ((rc = dupload(e, &gsr, a->gamma_s_real, (size_t)(d + 1) * C))) return rc;
-  if ((rc = dupload(e, &gsi, a->gamma_s_imag, (size_t)(d + 1) * C))) return rc;
-  if ((rc = dupload(e, &wts, a->wts, (size_t)2 * C * R))) return rc;
-  if ((rc = dupload(e, &shf, a->shifts, (size_t)2 * m * C * R))) return rc;
+  {
+    const int se = e->scale_exp;
+    std::vector<double> g(a->gamma, a->gamma + d + 1);
+    std::vector<double> gr(a->gamma_s_real, a->gamma_s_real + (size_t)(d + 1) * C);
+    std::vector<double> gi(a->gamma_s_imag, a->gamma_s_imag + (size_t)(d + 1) * C);
+    std::vector<double> w(a->wts, a->wts + (size_t)2 * C * R);
+    std::vector<double> sh(a->shifts, a->shifts + (size_t)2 * m * C * R);
+    if (se != 0) {
+      for (int i = 0; i <= d; ++i) {
+        g[i] = std::ldexp(g[i], se * (d - i));
+        for (int j = 0; j < C; ++j) {
+          gr[i + (size_t)(d + 1) * j] = std::ldexp(gr[i + (size_t)(d + 1) * j], se * (d - i));
+          gi[i + (size_t)(d + 1) * j] = std::ldexp(gi[i + (size_t)(d + 1) * j], se * (d - i));
+        }
+      }
+      for (auto& v : w) v = std::ldexp(v, -se);
+      for (auto& v : sh) v = std::ldexp(v, -se);
+    }
+    if ((rc = dupload(e, &gam, g.data(), d + 1))) return rc;
+    if ((rc = dupload(e, &gsr, gr.data(), gr.size()))) return rc;
+    if ((rc = dupload(e, &gsi, gi.data(), gi.size()))) return rc;
+    if ((rc = dupload(e, &wts, w.data(), w.size()))) return rc;
+    if ((rc = dupload(e, &shf, sh.data(), sh.size()))) return rc;
+  }
   if (k > 0) {
     if ((rc = dupload(e, &flam, a->flam, (size_t)k * R))) return rc;
     if ((rc = dupload(e, &Q, a->Q, (size_t)k * n))) return rc;
@@ -584,7 +621,15 @@ int gm_get_solution(gm_handle h, double* dst) {
 int gm_get_aabb(gm_handle h, double* dst) {
   if (!h || !dst) return GM_ERR_ARG;
   GM_CUDA(h, cudaMemcpyAsync(dst, h->kp.aabb, (size_t)(h->m + 1) * 2 * h->R * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-  return check_sync(h);
+  int rc = check_sync(h);
+  if (h->scale_exp != 0) {
+    // alpha_j and beta_{j>=1} of the scaled operator are those of A over 2^e
+    const size_t ld = h->m + 1;
+    for (int r = 0; r < 2 * h->R; ++r)
+      for (size_t q = 0; q < ld; ++q)
+        if (r < h->R || q > 0) dst[r * ld + q] = std::ldexp(dst[r * ld + q], h->scale_exp);
+  }
+  return rc;
 }
 
 int gm_get_y(gm_handle h, double* yr, double* yi) {
@@ -617,6 +662,7 @@ static int set_U_common(gm_handle h, const double* U, bool on_device) {
   int rc = set_usol(h, U, on_device);
   if (rc) return rc;
   GM_CUDA(h, cudaMemsetAsync(h->kp.status, 0, sizeof(int), h->stream));
+  GM_CUDA(h, cudaMemsetAsync(h->kp.bar, 0, sizeof(unsigned), h->stream));
   h->have_V = h->have_y = h->have_coef = false;
   return launch(h, gm::PH_DEFLATE, 0);
 }

@@ -95,24 +95,44 @@ __device__ __forceinline__ long long slot_row(const KParams& kp, long long s, in
 }
 
 // acc[r] = sum_j A(row, col_j) x[col_j][r] over the slice row of this lane.
+// The slice's columns are walked in chunks of CH: all CH column indices and
+// values are loaded first (coalesced, read-only path), then all CH gathers of
+// x are issued, then the CH products are accumulated, so each chunk costs two
+// memory latencies instead of 2*CH.
 template <class Pol, int R, class XT>
 __device__ __forceinline__ void spmv_slot(const KParams& kp, long long s, int lane, const XT* __restrict__ x,
                                           typename Pol::AT (&acc)[R]) {
   using VT = typename Pol::VT;
+  constexpr int CH = (R == 1) ? 8 : 4;
   const long long base = kp.slice_off[s];
   const int len = (int)((kp.slice_off[s + 1] - base) >> 5);
   const int* cp = kp.col + base + lane;
   const VT* vp = reinterpret_cast<const VT*>(kp.val) + base + lane;
 #pragma unroll
   for (int r = 0; r < R; ++r) acc[r] = Pol::zero();
-#pragma unroll 4
-  for (int jj = 0; jj < len; ++jj) {
-    const int c = __ldg(cp + (long long)jj * 32);
-    const VT a = __ldg(vp + (long long)jj * 32);
-    XT xv[R];
-    VecIO<R>::ld(x + (long long)c * R, xv);
+  for (int jj = 0; jj < len; jj += CH) {
+    int cc[CH];
+    VT aa[CH];
 #pragma unroll
-    for (int r = 0; r < R; ++r) acc[r] = Pol::acc(acc[r], a, xv[r]);
+    for (int u = 0; u < CH; ++u) {
+      if (jj + u < len) {
+        cc[u] = __ldg(cp + (long long)(jj + u) * 32);
+        aa[u] = __ldg(vp + (long long)(jj + u) * 32);
+      } else {
+        cc[u] = 0;
+        aa[u] = (VT)0;
+      }
+    }
+    XT xv[CH][R];
+#pragma unroll
+    for (int u = 0; u < CH; ++u)
+      if (jj + u < len) VecIO<R>::ld(x + (long long)cc[u] * R, xv[u]);
+#pragma unroll
+    for (int u = 0; u < CH; ++u)
+      if (jj + u < len) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[r] = Pol::acc(acc[r], aa[u], xv[u][r]);
+      }
   }
 }
 

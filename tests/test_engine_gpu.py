@@ -173,6 +173,24 @@ def test_fe_circle_golden(engine_lib, case):
     assert rel(x, g[f"{case}_x_pow"]) < 1e-6
 
 
+@pytest.mark.parametrize("degree", [0, 4])
+def test_mixed_precision_large_scale_operator(engine_lib, degree):
+    """h^-2-scaled operator with a degree-4 polynomial: the polynomial
+    coefficients and A^4 leave FP32's range unless the engine rescales."""
+    N = 48
+    P = workloads.fd2d_problem(N, 4, 40, 32, [params.frac_power(-0.8)], R=1, scale=1e6 * (N + 1.0) ** 2,
+                               seed=3, degree=degree)
+    want = oracle_for(P).solve()
+    eng = Engine.from_problem(P, precision="mixed")
+    eng.solve()
+    assert rel(eng.get_solution(), want) < MIXED_TOL
+    e64 = Engine.from_problem(P, precision="fp64")
+    e64.build_subspace()
+    eng.build_subspace()
+    ab, ab64 = eng.get_aabb(), e64.get_aabb()
+    assert rel(ab[:5], ab64[:5]) < 1e-5
+
+
 def test_mixed_precision_config1_small(engine_lib):
     P = workloads.config1_small(N=32, k=4, m=60, C=32, R=2, degree=0, seed=4)
     ora = oracle_for(P)
@@ -207,11 +225,29 @@ def test_breakdown_eigenvector_rhs(engine_lib):
     f = params.frac_exp(0.1, 1.5)
     P = workloads.make_problem("bd", A, b[:, None], np.zeros((N * N, 0)), np.zeros(0), [f], m=20, C=40,
                                l1=float(lam[0]) * 0.9, lN=8.0, degree=0)
-    eng = Engine.from_problem(P)
+    # rounding residue of the analytic eigenvectors grows to beta_3 ~ 2e-12
+    eng = Engine.from_problem(P, breakdown_tol=1e-10)
     eng.solve()
     assert eng.meff()[0] == 3
     x = eng.get_solution()[:, 0]
     assert rel(x, known.dense_fab(A, b, f)) < 1e-9
+
+
+def test_exact_breakdown_default_tolerance(engine_lib):
+    """Diagonal A and b on 3 coordinates: the Krylov space is exactly
+    3-dimensional, beta_3 is at rounding level and the default tolerance stops."""
+    n = 64
+    d = np.linspace(1.0, 10.0, n)
+    A = sp.diags(d).tocsr()
+    b = np.zeros(n)
+    b[[3, 20, 50]] = [1.0, -2.0, 0.5]
+    f = params.frac_power(-0.8)
+    P = workloads.make_problem("diag", A, b[:, None], np.zeros((n, 0)), np.zeros(0), [f], m=12, C=40,
+                               l1=0.9, lN=11.0, degree=0)
+    eng = Engine.from_problem(P)
+    eng.solve()
+    assert eng.meff()[0] == 3
+    assert rel(eng.get_solution()[:, 0], f(d) * b) < 1e-9
 
 
 def test_zero_rhs(engine_lib):
