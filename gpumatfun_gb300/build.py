@@ -16,7 +16,7 @@ CSRC = PKG / "csrc"
 LIBDIR = PKG / "_lib"
 LIB = LIBDIR / "libgpumatfun.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["engine.cu", "kern_fp64.cu", "kern_mixed.cu"]
+SOURCES = ["engine.cu", "kern_fp64.cu", "kern_mixed.cu", "noalloc.cu"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC"]
 
 

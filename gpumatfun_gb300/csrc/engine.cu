@@ -525,6 +525,12 @@ int create_impl(const gm_create_args* a, gm_engine* e) {
 
 }  // namespace
 
+namespace gm {
+// Sets the message gm_last_error(NULL) returns (used by entry points that
+// have no handle).
+void set_global_error(const char* msg) { g_create_error = msg ? msg : ""; }
+}  // namespace gm
+
 // ====================================================================== C ABI
 extern "C" {
 

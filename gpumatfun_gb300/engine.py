@@ -33,6 +33,7 @@ EXPORTED_SYMBOLS = [
     "gm_get_xsol", "gm_get_aabb", "gm_set_y", "gm_get_y", "gm_set_U", "gm_set_U_device", "gm_get_update",
     "gm_get_solution", "gm_solve", "gm_solve_host", "gm_sync", "gm_set_stream",
     "gm_phase_times", "gm_info", "gm_get_meff", "gm_last_error", "gm_version",
+    "gm_lin_sys_solves_noalloc",
 ]
 
 _dp = ct.POINTER(ct.c_double)

@@ -203,6 +203,36 @@ int gm_info(gm_handle h, int64_t* info12);
  * breakdown). */
 int gm_get_meff(gm_handle h, int* meff);
 
+/* Largest m * nrhs * C accepted by gm_lin_sys_solves_noalloc. */
+#define GM_NOALLOC_MAX_ENTRIES 32768
+
+/* The shifted tridiagonal solves of gm_lin_sys_solves for callers that
+ * cannot allocate device memory -- applications whose device memory is all
+ * owned by their own allocator (MATLAB's gpuArray manager, a framework's
+ * caching pool, a fixed-budget embedded solver) and latency-critical loops
+ * where cudaMalloc's implicit device synchronisation is not acceptable.  No
+ * counterpart in the reference.
+ *
+ * All pointers are device pointers on the current device, supplied by the
+ * caller: aabb ((m+1) x 2*nrhs, column-major, alpha columns then beta
+ * columns, as gm_get_aabb returns), meff (nrhs ints, clamped to [0, m];
+ * NULL = m), wts
+ * (nrhs blocks of C x 2 [re, im]), shifts (2*m*C*nrhs) and the outputs
+ * yreal, yimag (m x nrhs*C, as gm_get_y).  stream is a cudaStream_t (NULL =
+ * legacy default stream); the call is asynchronous on it.
+ *
+ * The only other memory used is a fixed table of 1 MiB + 32 bytes in a
+ * file-scope __device__ array, so m * nrhs * C must not exceed
+ * GM_NOALLOC_MAX_ENTRIES (GM_ERR_ARG otherwise, message in
+ * gm_last_error(NULL)).  The first call on a device looks up the table's
+ * device address (once per device, with that device current); make that
+ * first call before any stream capture.  All calls share the table and it
+ * keeps the last call's contents (no entry needs to start at zero): calls
+ * whose kernels overlap on the GPU race and must be ordered on one stream. */
+int gm_lin_sys_solves_noalloc(int m, int nrhs, int contour_size, const double* aabb, const int* meff,
+                              const double* wts, const double* shifts, double* yreal, double* yimag,
+                              void* stream);
+
 /* Last error message of h (or of the last failed create when h is NULL). */
 const char* gm_last_error(gm_handle h);
 
