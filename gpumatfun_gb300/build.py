@@ -14,10 +14,14 @@ from pathlib import Path
 PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 LIBDIR = PKG / "_lib"
-LIB = LIBDIR / "libgpumatfun.so"
+LIB = Path(os.environ["GPUMATFUN_LIB"]) if os.environ.get("GPUMATFUN_LIB") else LIBDIR / "libgpumatfun.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["engine.cu", "kern_fp64.cu", "kern_mixed.cu", "noalloc.cu"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC"]
+# Kernel shape overrides for tuning builds, e.g. "-DGM_MINB=1 -DGM_CH1=8"
+# (GM_MINB: minimum resident 512-thread blocks per SM; GM_CH1/2/4: SpMV chunk
+# width for 1/2/4 right-hand sides).
+EXTRA = os.environ.get("GPUMATFUN_NVCC_EXTRA", "").split()
 
 
 def nvcc_path() -> str:
@@ -39,14 +43,14 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     """Compile the engine library if it is missing or older than its sources."""
     if not force and not _stale():
         return LIB
-    LIBDIR.mkdir(exist_ok=True)
+    LIB.parent.mkdir(parents=True, exist_ok=True)
     nvcc = nvcc_path()
     tag = f"{os.getpid()}"
     objs, procs = [], []
     # one translation unit per precision so the kernel instantiations compile in parallel
     for src in SOURCES:
-        obj = LIBDIR / (Path(src).stem + f".{tag}.o")
-        cmd = [nvcc, *ARCH, *FLAGS, "-c", "-o", str(obj), str(CSRC / src)]
+        obj = LIB.parent / (Path(src).stem + f".{tag}.o")
+        cmd = [nvcc, *ARCH, *FLAGS, *EXTRA, "-c", "-o", str(obj), str(CSRC / src)]
         if verbose:
             print(" ".join(cmd))
         procs.append((subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True), src))

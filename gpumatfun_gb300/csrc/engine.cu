@@ -42,8 +42,11 @@ struct gm_engine {
   int R = 0, m = 0, d = 0, C = 0, k = 0, prec = 0, sync_mode = 1;
   int threads = 512, G = 0;
   int scale_exp = 0;             // mixed engine: A stored as A * 2^-scale_exp
+  unsigned long long epoch = 0;  // launch counter (progress-flag epochs)
+  double dep_avg = 0.0;          // mean neighbour-list length per block
   int Gk[5] = {};                // grid size per phase group (co-residency bound)
   void* kfn[5] = {};
+  size_t smem[5] = {};           // dynamic shared memory per phase group
   std::vector<DevBuf> bufs;
   size_t bytes = 0;
   KParams kp{};
@@ -166,12 +169,12 @@ int make_csr(gm_engine* e, const gm_create_args* a, Csr& out) {
 }
 
 template <class VT>
-int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp) {
+int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp, std::vector<long long>& rows,
+                std::vector<long long>& off) {
   const long long n = e->n;
   const long long nsl = (n + 31) / 32;
-  std::vector<int> perm;  // slot -> row
   bool sorted = sigma > 1;
-  std::vector<long long> rows(nsl * 32);
+  rows.assign(nsl * 32, -1);
   for (long long s = 0; s < nsl * 32; ++s) rows[s] = s < n ? s : -1;
   if (sorted) {
     for (long long w0 = 0; w0 < n; w0 += sigma) {
@@ -181,7 +184,7 @@ int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp) {
       });
     }
   }
-  std::vector<long long> off(nsl + 1, 0);
+  off.assign(nsl + 1, 0);
   for (long long s = 0; s < nsl; ++s) {
     long long L = 0;
     for (int l = 0; l < 32; ++l) {
@@ -235,6 +238,70 @@ int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp) {
   return GM_OK;
 }
 
+// Static partition of the SELL slices over the G blocks (contiguous ranges
+// balanced by padded entries plus a per-row cost) and, per block, the sorted
+// list of other blocks owning a row that one of its rows references, closed
+// under symmetry (see DepSync in fab_common.cuh).
+int build_partition(gm_engine* e, const Csr& A, const std::vector<long long>& rows,
+                    const std::vector<long long>& off) {
+  const long long nsl = (long long)off.size() - 1;
+  const int G = e->G;
+  std::vector<int> bs(G + 1, 0);
+  double total = 0.0;
+  for (long long s = 0; s < nsl; ++s) total += (double)(off[s + 1] - off[s]) + 32.0 * 4.0;
+  double acc = 0.0;
+  int b = 0;
+  for (long long s = 0; s < nsl; ++s) {
+    const double w = (double)(off[s + 1] - off[s]) + 32.0 * 4.0;
+    while (b < G - 1 && acc + 0.5 * w > total * (b + 1) / G) bs[++b] = (int)s;
+    acc += w;
+  }
+  while (b < G) bs[++b] = (int)nsl;
+  std::vector<int> owner(e->n, 0);
+  for (int q = 0; q < G; ++q)
+    for (long long s = bs[q]; s < bs[q + 1]; ++s)
+      for (int l = 0; l < 32; ++l) {
+        const long long r = rows[s * 32 + l];
+        if (r >= 0) owner[r] = q;
+      }
+  std::vector<unsigned char> adj((size_t)G * G, 0);
+  for (int q = 0; q < G; ++q)
+    for (long long s = bs[q]; s < bs[q + 1]; ++s)
+      for (int l = 0; l < 32; ++l) {
+        const long long r = rows[s * 32 + l];
+        if (r < 0) continue;
+        for (long long t = A.ptr[r]; t < A.ptr[r + 1]; ++t) {
+          const int o = owner[A.col[t]];
+          if (o != q) {
+            adj[(size_t)q * G + o] = 1;
+            adj[(size_t)o * G + q] = 1;
+          }
+        }
+      }
+  std::vector<int> dp(G + 1, 0), di;
+  for (int q = 0; q < G; ++q) {
+    for (int o = 0; o < G; ++o)
+      if (adj[(size_t)q * G + o]) di.push_back(o);
+    dp[q + 1] = (int)di.size();
+  }
+  e->dep_avg = G ? (double)di.size() / G : 0.0;
+  int* d_bs;
+  int* d_dp;
+  int* d_di;
+  unsigned long long* d_prog;
+  int rc;
+  if ((rc = dupload(e, &d_bs, bs.data(), bs.size()))) return rc;
+  if ((rc = dupload(e, &d_dp, dp.data(), dp.size()))) return rc;
+  if ((rc = dupload(e, &d_di, di.data(), di.size()))) return rc;
+  if ((rc = dalloc(e, &d_prog, (size_t)G))) return rc;
+  GM_CUDA(e, cudaMemset(d_prog, 0, sizeof(unsigned long long) * G));
+  e->kp.blk_slice = d_bs;
+  e->kp.dep_ptr = d_dp;
+  e->kp.dep_idx = d_di;
+  e->kp.prog = d_prog;
+  return GM_OK;
+}
+
 // Phase-group kernels (kern_fp64.cu / kern_mixed.cu): 0 lanczos, 1 solves,
 // 2 apply, 3 deflate/update, 4 fused lanczos + solves + apply.
 enum { KGRP_LANCZOS = 0, KGRP_SOLVE = 1, KGRP_APPLY = 2, KGRP_DEFLATE = 3, KGRP_FUSED = 4, KGRP_N = 5 };
@@ -281,7 +348,8 @@ int launch(gm_engine* e, int phases, int slot) {
   GM_CUDA(e, cudaEventRecord(e->ev[slot][0], e->stream));
   const int grp = group_of(phases);
   kp.G = e->Gk[grp];
-  cudaError_t st = cudaLaunchCooperativeKernel(e->kfn[grp], dim3(kp.G), dim3(e->threads), args, 0, e->stream);
+  kp.epoch = ++e->epoch;
+  cudaError_t st = cudaLaunchCooperativeKernel(e->kfn[grp], dim3(kp.G), dim3(e->threads), args, e->smem[grp], e->stream);
   if (st != cudaSuccess) return cuda_fail(e, st, "cudaLaunchCooperativeKernel");
   GM_CUDA(e, cudaEventRecord(e->ev[slot][1], e->stream));
   e->ev_used[slot] = true;
@@ -368,27 +436,6 @@ int create_impl(const gm_create_args* a, gm_engine* e) {
     for (int t = 0; t < 2; ++t) GM_CUDA(e, cudaEventCreate(&e->ev[s][t]));
   GM_CUDA(e, cudaHostAlloc((void**)&e->h_status, sizeof(int) * 8, cudaHostAllocDefault));
 
-  // Grid: blocks_per_sm x SMs, capped by co-residency of each phase-group
-  // kernel and by the work (about one SELL slice per warp: small problems
-  // get fewer blocks, which makes every grid barrier cheaper).
-  const long long nsl = (e->n + 31) / 32;
-  const int nw = e->threads / 32;
-  const long long want = std::max<long long>(1, (nsl + nw - 1) / nw);
-  long long Gmax = 0;
-  for (int g = 0; g < KGRP_N; ++g) {
-    e->kfn[g] = pick_kernel(e->prec, e->R, g);
-    if (!e->kfn[g]) return fail(e, GM_ERR_UNSUPPORTED, "no kernel for nrhs %d", e->R);
-    int nb = 0;
-    GM_CUDA(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, e->kfn[g], e->threads, 0));
-    if (nb < 1) return fail(e, GM_ERR_UNSUPPORTED, "kernel group %d cannot be resident with %d threads", g, e->threads);
-    const int bps = a->blocks_per_sm > 0 ? std::min(a->blocks_per_sm, nb) : nb;
-    long long G = (long long)bps * e->nsm;
-    if (a->blocks_per_sm <= 0) G = std::min(G, want);
-    e->Gk[g] = (int)std::max<long long>(1, G);
-    Gmax = std::max(Gmax, (long long)e->Gk[g]);
-  }
-  e->G = (int)Gmax;
-
   int rc;
   Csr csr;
   if ((rc = make_csr(e, a, csr))) return rc;
@@ -407,9 +454,45 @@ int create_impl(const gm_create_args* a, gm_engine* e) {
     }
     e->scale_exp = mx > 0.0 ? (int)std::floor(std::log2(mx)) : 0;
   }
-  rc = e->prec == GM_FP64 ? upload_sell<double>(e, csr, a->sell_sigma, 0)
-                          : upload_sell<float>(e, csr, a->sell_sigma, e->scale_exp);
+  std::vector<long long> slot_rows, slice_off;
+  rc = e->prec == GM_FP64 ? upload_sell<double>(e, csr, a->sell_sigma, 0, slot_rows, slice_off)
+                          : upload_sell<float>(e, csr, a->sell_sigma, e->scale_exp, slot_rows, slice_off);
   if (rc) return rc;
+  // Column staging: per warp two stages of stage_cap * 32 column indices
+  // (slices with more columns are read from global memory directly).
+  long long max_len = 0;
+  for (size_t q = 0; q + 1 < slice_off.size(); ++q) max_len = std::max(max_len, (slice_off[q + 1] - slice_off[q]) / 32);
+  const int stage_cap = a->col_staging == 0 ? (int)std::min<long long>(max_len, 24) : 0;
+  const size_t stage_smem = stage_cap > 0 ? (size_t)16 * (e->threads / 32) + (size_t)2 * (e->threads / 32) * stage_cap * 128 : 0;
+  e->kp.stage_cap = stage_cap;
+  // Grid: blocks_per_sm x SMs, capped by co-residency of each phase-group
+  // kernel and by the work (about one SELL slice per warp: small problems
+  // get fewer blocks, which makes every grid barrier cheaper).
+  const long long nsl = (e->n + 31) / 32;
+  const int nw = e->threads / 32;
+  const long long want = std::max<long long>(1, (nsl + nw - 1) / nw);
+  long long Gmax = 0;
+  for (int g = 0; g < KGRP_N; ++g) {
+    e->kfn[g] = pick_kernel(e->prec, e->R, g);
+    if (!e->kfn[g]) return fail(e, GM_ERR_UNSUPPORTED, "no kernel for nrhs %d", e->R);
+    e->smem[g] = (g == KGRP_LANCZOS || g == KGRP_APPLY || g == KGRP_FUSED) ? stage_smem : 0;
+    if (e->smem[g] > 48 * 1024)
+      GM_CUDA(e, cudaFuncSetAttribute(e->kfn[g], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem[g]));
+    int nb = 0;
+    GM_CUDA(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, e->kfn[g], e->threads, e->smem[g]));
+    if (nb < 1) return fail(e, GM_ERR_UNSUPPORTED, "kernel group %d cannot be resident with %d threads", g, e->threads);
+    const int bps = a->blocks_per_sm > 0 ? std::min(a->blocks_per_sm, nb) : nb;
+    long long G = (long long)bps * e->nsm;
+    if (a->blocks_per_sm <= 0) G = std::min(G, want);
+    e->Gk[g] = (int)std::max<long long>(1, G);
+    Gmax = Gmax == 0 ? e->Gk[g] : std::min(Gmax, (long long)e->Gk[g]);
+  }
+  // one grid size for every group: the slice partition is per block
+  for (int g = 0; g < KGRP_N; ++g) e->Gk[g] = (int)Gmax;
+  e->G = (int)Gmax;
+
+  if ((rc = build_partition(e, csr, slot_rows, slice_off))) return rc;
+  e->kp.dep_mode = a->sync_policy == 0 ? 1 : 0;
   csr = Csr();
 
   KParams& kp = e->kp;

@@ -259,6 +259,102 @@ struct GridBar {
   }
 };
 
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
+// Dependency-local ordering between consecutive SpMV passes.  Block b owns a
+// contiguous range of SELL slices; dep_idx[dep_ptr[b]..dep_ptr[b+1]) lists the
+// blocks owning any row that b's rows reference, closed under symmetry.  After
+// a pass, a block publishes (epoch << 20) + pass in prog[b]; before the next
+// gathering pass it waits only for its neighbours.  Symmetry also makes the
+// ping-pong buffer reuse safe: a neighbour that finished pass k-1 has finished
+// reading this block's rows of the buffer pass k overwrites.  The epoch is the
+// launch counter, so values left by earlier launches never satisfy a wait.
+// Waits are bounded like GridBar's.
+struct DepSync {
+  unsigned long long* prog;
+  const int* dep_ptr;
+  const int* dep_idx;
+  int* status;
+  unsigned long long base;   // epoch << 20
+  unsigned long long timeout_ns;
+
+  __device__ void publish(unsigned pass) const {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      st_release_u64(prog + blockIdx.x, base + pass);
+    }
+  }
+
+  __device__ bool wait(unsigned pass) const {
+    __shared__ int s_ok;
+    const unsigned long long want = base + pass;
+    if (threadIdx.x < 32) {
+      int ok = 1;
+      const int t0 = dep_ptr[blockIdx.x], t1 = dep_ptr[blockIdx.x + 1];
+      for (int t = t0 + (int)threadIdx.x; t < t1 && ok; t += 32) {
+        const unsigned long long* p = prog + dep_idx[t];
+        unsigned long long start = 0;
+        unsigned spins = 0;
+        while (ld_acquire_u64(p) < want) {
+          if ((++spins & 31u) == 0) {
+            if (*(volatile int*)status != 0) { ok = 0; break; }
+            const unsigned long long now = global_timer_ns();
+            if (start == 0) {
+              start = now;
+            } else if (now - start > timeout_ns) {
+              atomicCAS(status, 0, (int)ST_TIMEOUT);
+              ok = 0;
+              break;
+            }
+          }
+          __nanosleep(20);
+        }
+      }
+      ok = __all_sync(0xffffffffu, ok);
+      if (threadIdx.x == 0) s_ok = ok && (*(volatile int*)status == 0);
+    }
+    __syncthreads();
+    return s_ok != 0;
+  }
+};
+
+// ---------------------------------------------------------------- TMA bulk copies
+// Untiled bulk copy global -> shared completed on an mbarrier (the Blackwell
+// TMA engine; both addresses 16-byte aligned, size a multiple of 16 bytes).
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_init_fence() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void tma_bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+               ::"r"(smem_addr(dst)), "l"(src), "r"(bytes), "r"(smem_addr(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile("{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+               : "=r"(ok) : "r"(smem_addr(bar)), "r"(parity) : "memory");
+  return ok != 0;
+}
+
 // ---------------------------------------------------------------- reductions
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

@@ -70,6 +70,14 @@ struct KParams {
   double* Z;
   double* part;     // [2R + k R][G]
   unsigned* bar;    // [0] count, [1] generation
+  const int* blk_slice;       // [G+1] slice range owned by each block
+  const int* dep_ptr;         // [G+1] neighbour list of each block
+  const int* dep_idx;
+  unsigned long long* prog;   // [G] pass progress flags
+  unsigned long long epoch;   // launch counter
+  int dep_mode;               // 1: neighbour waits between SpMV passes, 0: grid barriers
+  int stage_cap;              // >0: stage each slice's column indices in shared memory by TMA
+                              // bulk copies (slices of at most stage_cap columns); 0: off
   int* status;
   int* meff;        // [R]
   unsigned long long timeout_ns;
@@ -87,6 +95,29 @@ struct Ctx {
   }
 };
 
+__device__ __forceinline__ DepSync make_dep(const KParams& kp) {
+  return DepSync{kp.prog, kp.dep_ptr, kp.dep_idx, kp.status, kp.epoch << 20, kp.timeout_ns};
+}
+
+// Orders consecutive SpMV passes: after pass pc (published), the next
+// gathering pass waits for the neighbours' pass pc (or a grid barrier).  One
+// PassSync lives for the whole launch and is shared by all phases, so pass
+// numbers keep increasing across phases: a phase that restarted at 0 would
+// find its waits already satisfied by flags published earlier in the launch.
+struct PassSync {
+  GridBar bar;
+  DepSync dep;
+  int mode;
+  unsigned pc;
+  __device__ void done() {
+    ++pc;
+    if (mode) dep.publish(pc);
+  }
+  __device__ bool before_next() {
+    return mode ? dep.wait(pc) : bar.sync();
+  }
+};
+
 // Row of SELL slot (slice s, lane); -1 for padding.
 __device__ __forceinline__ long long slot_row(const KParams& kp, long long s, int lane) {
   long long slot = s * 32 + lane;
@@ -99,11 +130,32 @@ __device__ __forceinline__ long long slot_row(const KParams& kp, long long s, in
 // values are loaded first (coalesced, read-only path), then all CH gathers of
 // x are issued, then the CH products are accumulated, so each chunk costs two
 // memory latencies instead of 2*CH.
+// Chunk width: one column index, one value and R gathered entries are live
+// per chunk element across the gathers.  These widths are the largest that
+// compile without local-memory spills at the kernel's 128-register bound
+// (checked with -Xptxas -v for every instantiation).
+#ifndef GM_CH1
+#define GM_CH1 4
+#endif
+#ifndef GM_CH2
+#define GM_CH2 2
+#endif
+#ifndef GM_CH4
+#define GM_CH4 2
+#endif
+#ifndef GM_CH4F
+#define GM_CH4F 3
+#endif
+template <class VT, class XT, int R>
+struct ChunkWidth {
+  static constexpr int value = R == 1 ? GM_CH1 : (R == 2 ? GM_CH2 : (sizeof(VT) == 8 ? GM_CH4 : GM_CH4F));
+};
+
 template <class Pol, int R, class XT>
 __device__ __forceinline__ void spmv_slot(const KParams& kp, long long s, int lane, const XT* __restrict__ x,
-                                          typename Pol::AT (&acc)[R]) {
+                                          typename Pol::AT (&acc)[R], const int* scol = nullptr) {
   using VT = typename Pol::VT;
-  constexpr int CH = (R == 1) ? 8 : 4;
+  constexpr int CH = ChunkWidth<VT, XT, R>::value;
   const long long base = kp.slice_off[s];
   const int len = (int)((kp.slice_off[s + 1] - base) >> 5);
   const int* cp = kp.col + base + lane;
@@ -116,7 +168,7 @@ __device__ __forceinline__ void spmv_slot(const KParams& kp, long long s, int la
 #pragma unroll
     for (int u = 0; u < CH; ++u) {
       if (jj + u < len) {
-        cc[u] = __ldg(cp + (long long)(jj + u) * 32);
+        cc[u] = scol ? scol[(jj + u) * 32 + lane] : __ldg(cp + (long long)(jj + u) * 32);
         aa[u] = __ldg(vp + (long long)(jj + u) * 32);
       } else {
         cc[u] = 0;
@@ -140,18 +192,148 @@ template <class Pol> __device__ __forceinline__ typename Pol::AT h_load_at(const
 template <> __device__ __forceinline__ double h_load_at<PolFP64>(const double& h) { return h; }
 template <> __device__ __forceinline__ ff h_load_at<PolMixed>(const float2& h) { return {h.x, h.y}; }
 
+// Per-warp double-buffered staging of SELL column indices.  Lane 0 issues a
+// TMA bulk copy of the next slice's column block (128 bytes per slice column,
+// contiguous in the SELL layout) into shared memory while the warp computes
+// the current slice, so a slice costs one global round trip (values and x
+// gathers together) instead of two.  Dynamic shared memory holds, per warp,
+// two mbarriers and two stages of stage_cap * 32 ints.
+struct ColStage {
+  int* buf0;
+  int* buf1;
+  unsigned long long* bar0;
+  unsigned long long* bar1;
+  unsigned phase;     // bit k: parity of stage k's next completion
+  unsigned issued;    // bit k: stage k holds an outstanding copy
+  int cap;
+
+  __device__ void init(const KParams& kp, const Ctx& c) {
+    cap = kp.stage_cap;
+    phase = 0u;
+    issued = 0u;
+    if (cap <= 0) return;
+    extern __shared__ __align__(128) unsigned char dsm[];
+    unsigned long long* bars = reinterpret_cast<unsigned long long*>(dsm);
+    int* bufs = reinterpret_cast<int*>(dsm + 16 * c.nw);
+    bar0 = bars + 2 * c.warp;
+    bar1 = bar0 + 1;
+    buf0 = bufs + (long long)(2 * c.warp) * cap * 32;
+    buf1 = buf0 + (long long)cap * 32;
+    if (c.lane == 0) {
+      mbar_init(bar0, 1);
+      mbar_init(bar1, 1);
+      mbar_init_fence();
+    }
+    __syncwarp();
+  }
+
+  // stage k <- columns of slice s (lane 0 issues; warp-uniform bookkeeping)
+  __device__ void issue(const KParams& kp, int k, long long s, int lane) {
+    if (cap <= 0) return;
+    const long long base = kp.slice_off[s];
+    const int len = (int)((kp.slice_off[s + 1] - base) >> 5);
+    if (len <= 0 || len > cap) return;
+    if (lane == 0) {
+      unsigned long long* bar = k ? bar1 : bar0;
+      const unsigned bytes = 128u * (unsigned)len;
+      mbar_arrive_expect_tx(bar, bytes);
+      tma_bulk_g2s(k ? buf1 : buf0, kp.col + base, bytes, bar);
+    }
+    issued |= 1u << k;
+  }
+
+  // Waits for stage k; returns its buffer, or nullptr when the slice is read
+  // from global memory (not staged) or the wait ran out (status recorded).
+  __device__ const int* ready(const KParams& kp, int k, int lane) {
+    if (!(issued & (1u << k))) return nullptr;
+    unsigned long long* bar = k ? bar1 : bar0;
+    const unsigned par = (phase >> k) & 1u;
+    unsigned long long start = 0;
+    bool timed_out = false;
+    while (!mbar_try_wait(bar, par)) {
+      const unsigned long long now = global_timer_ns();
+      if (start == 0) {
+        start = now;
+      } else if (!timed_out && now - start > kp.timeout_ns) {
+        if (lane == 0) atomicCAS(kp.status, 0, (int)ST_TIMEOUT);
+        timed_out = true;
+        start = now;  // keep waiting a bounded time for the copy in flight
+      } else if (timed_out && now - start > kp.timeout_ns) {
+        break;
+      }
+    }
+    phase ^= 1u << k;
+    issued &= ~(1u << k);
+    return timed_out ? nullptr : (k ? buf1 : buf0);
+  }
+
+  // all lanes are done reading stage k before a later copy overwrites it
+  __device__ void release() {
+    if (cap <= 0) return;
+    fence_proxy_async_smem();
+    __syncwarp();
+  }
+};
+
+// One SpMV pass over the block's slices: z = A x for the slice rows, then
+// epi(s, z) for the row epilogue.
+template <class Pol, int R, class XT, class Epi>
+__device__ __forceinline__ void spmv_pass(const KParams& kp, const Ctx& c, ColStage& cs, const XT* x, Epi&& epi) {
+  using AT = typename Pol::AT;
+  const long long sb = kp.blk_slice[c.b], se = kp.blk_slice[c.b + 1];
+  long long s = sb + c.warp;
+  if (s < se) cs.issue(kp, 0, s, c.lane);
+  int k = 0;
+  for (; s < se; s += c.nw, k ^= 1) {
+    const long long sn = s + c.nw;
+    if (sn < se) cs.issue(kp, k ^ 1, sn, c.lane);
+    const int* scol = cs.ready(kp, k, c.lane);
+    AT z[R];
+    spmv_slot<Pol, R, XT>(kp, s, c.lane, x, z, scol);
+    epi(s, z);
+    cs.release();
+  }
+}
+
 // ------------------------------------------------------------------ LANCZOS
 // build_subspace.cu:5-89 with the three-term recurrence as two grid passes
 // per step (A: SpMV + beta_j v_{j-1} + alpha partials; B: w -= alpha v_j +
 // beta partials), plus d Horner passes for the polynomial preconditioner.
 // v_{j+1} = w (1/beta_{j+1}) is formed on the fly in the next step's first
 // pass, which also stores it in V.
+// Block-uniform Lanczos scalars live in shared memory, not registers: with R
+// right-hand sides they would otherwise occupy ~10R registers across every
+// SpMV pass and push the passes into local-memory spills.
 template <class Pol, int R>
-__device__ bool phase_lanczos(const KParams& kp, const Ctx& c) {
+struct LanczosScalars {
+  double beta[R], rbeta[R], alpha[R], tot[R];
+  int broken[R];
+  typename Pol::ST sc[R], rb[R], bj[R], al[R];
+  int all_broken;
+};
+
+// Every block sums the G per-block partials (layout [R][G]) in one fixed
+// order into dst (shared memory); deterministic and identical in all blocks.
+template <int N>
+__device__ __forceinline__ void grid_total_smem(const double* partials, int G, double* dst) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp == 0) {
+#pragma unroll
+    for (int j = 0; j < N; ++j) {
+      double t = 0.0;
+      for (int b = lane; b < G; b += 32) t += partials[(long long)j * G + b];
+      t = warp_sum(t);
+      if (lane == 0) dst[j] = t;
+    }
+  }
+  __syncthreads();
+}
+
+template <class Pol, int R>
+__device__ bool phase_lanczos(const KParams& kp, const Ctx& c, PassSync& ps, ColStage& cs) {
   using BT = typename Pol::BT;
   using HT = typename Pol::HT;
   using AT = typename Pol::AT;
-  using ST = typename Pol::ST;
   const long long n = kp.n;
   const int m = kp.m, d = kp.d, G = kp.G;
   GridBar bar{kp.bar, kp.bar + 1, kp.status, (unsigned)G, kp.timeout_ns};
@@ -162,6 +344,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c) {
   HT* const H1 = reinterpret_cast<HT*>(kp.H1);
   double* part_a = kp.part;
   double* part_b = kp.part + (long long)R * G;
+  __shared__ LanczosScalars<Pol, R> sh;
 
   // prologue: W1 = U (storage precision), beta_0 = ||U_r||
   {
@@ -179,188 +362,179 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c) {
     block_sum_store<R>(bp, part_b + c.b, G);
   }
   if (!bar.sync()) return false;
-  double beta[R], rbeta[R];
-  bool broken[R];
-  {
-    double tot[R];
-    grid_total<R>(part_b, G, tot);
-#pragma unroll
+  grid_total_smem<R>(part_b, G, sh.tot);
+  if (c.tid == 0) {
     for (int r = 0; r < R; ++r) {
-      beta[r] = sqrt(tot[r]);
-      broken[r] = !(beta[r] > 0.0);
-      rbeta[r] = broken[r] ? 0.0 : 1.0 / beta[r];
-    }
-    if (c.b == 0 && c.tid == 0) {
-#pragma unroll
-      for (int r = 0; r < R; ++r) {
-        kp.aabb[(long long)(m + 1) * (R + r)] = beta[r];
-        kp.meff[r] = broken[r] ? 0 : m;
-        if (!(tot[r] == tot[r]) || isinf(tot[r])) atomicCAS(kp.status, 0, (int)ST_NONFINITE);
+      sh.beta[r] = sqrt(sh.tot[r]);
+      sh.broken[r] = !(sh.beta[r] > 0.0);
+      sh.rbeta[r] = sh.broken[r] ? 0.0 : 1.0 / sh.beta[r];
+      if (c.b == 0) {
+        kp.aabb[(long long)(m + 1) * (R + r)] = sh.beta[r];
+        kp.meff[r] = sh.broken[r] ? 0 : m;
+        if (!(sh.tot[r] == sh.tot[r]) || isinf(sh.tot[r])) atomicCAS(kp.status, 0, (int)ST_NONFINITE);
       }
     }
   }
+  __syncthreads();
   const BT* src = W1;
   for (int j = 0; j < m; ++j) {
     BT* Vj = V + (long long)j * n * R;
     const BT* Vjm1 = j > 0 ? V + (long long)(j - 1) * n * R : V;
     BT* Wout = (j & 1) ? W1 : W0;
-    ST sc[R], rb[R], bj[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      sc[r] = Pol::scalar(rbeta[r] * kp.gamma[0]);
-      rb[r] = Pol::scalar(rbeta[r]);
-      bj[r] = Pol::scalar(beta[r]);
+    if (c.tid == 0) {
+      for (int r = 0; r < R; ++r) {
+        sh.sc[r] = Pol::scalar(sh.rbeta[r] * kp.gamma[0]);
+        sh.rb[r] = Pol::scalar(sh.rbeta[r]);
+        sh.bj[r] = Pol::scalar(sh.beta[r]);
+      }
     }
+    __syncthreads();
     AT apa[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) apa[r] = Pol::zero();
     if (d == 0) {
-      for (long long s = c.gw; s < kp.nslices; s += c.tw) {
-        AT z[R];
-        spmv_slot<Pol, R, BT>(kp, s, c.lane, src, z);
+      spmv_pass<Pol, R, BT>(kp, c, cs, src, [&](long long s, AT (&z)[R]) {
         const long long row = slot_row(kp, s, c.lane);
-        if (row >= 0) {
-          BT sv[R], v[R];
-          VecIO<R>::ld(src + row * R, sv);
+        if (row < 0) return;
+        BT sv[R], v[R];
+        VecIO<R>::ld(src + row * R, sv);
 #pragma unroll
-          for (int r = 0; r < R; ++r) v[r] = Pol::scale_to_b(sv[r], rb[r]);
-          VecIO<R>::st(Vj + row * R, v);
-          AT w[R];
+        for (int r = 0; r < R; ++r) v[r] = Pol::scale_to_b(sv[r], sh.rb[r]);
+        VecIO<R>::st(Vj + row * R, v);
+        AT w[R];
 #pragma unroll
-          for (int r = 0; r < R; ++r) w[r] = Pol::mul(z[r], sc[r]);
-          if (j > 0) {
-            BT vp[R];
-            VecIO<R>::ld(Vjm1 + row * R, vp);
+        for (int r = 0; r < R; ++r) w[r] = Pol::mul(z[r], sh.sc[r]);
+        if (j > 0) {
+          BT vp[R];
+          VecIO<R>::ld(Vjm1 + row * R, vp);
 #pragma unroll
-            for (int r = 0; r < R; ++r) w[r] = Pol::sub_mul(w[r], bj[r], vp[r]);
-          }
-          BT wb[R];
-#pragma unroll
-          for (int r = 0; r < R; ++r) { wb[r] = Pol::to_b(w[r]); apa[r] = Pol::dot(apa[r], w[r], v[r]); }
-          VecIO<R>::st(Wout + row * R, wb);
+          for (int r = 0; r < R; ++r) w[r] = Pol::sub_mul(w[r], sh.bj[r], vp[r]);
         }
-      }
+        BT wb[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) { wb[r] = Pol::to_b(w[r]); apa[r] = Pol::dot(apa[r], w[r], v[r]); }
+        VecIO<R>::st(Wout + row * R, wb);
+      });
     } else {
       // Horner pass 1: u = gamma_1 v_j + A (gamma_0 v_j); stores v_j
       {
-        ST g1[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) g1[r] = Pol::scalar(kp.gamma[1]);
-        for (long long s = c.gw; s < kp.nslices; s += c.tw) {
-          AT z[R];
-          spmv_slot<Pol, R, BT>(kp, s, c.lane, src, z);
+        const typename Pol::ST g1 = Pol::scalar(kp.gamma[1]);
+        spmv_pass<Pol, R, BT>(kp, c, cs, src, [&](long long s, AT (&z)[R]) {
           const long long row = slot_row(kp, s, c.lane);
-          if (row >= 0) {
-            BT sv[R], v[R];
-            VecIO<R>::ld(src + row * R, sv);
+          if (row < 0) return;
+          BT sv[R], v[R];
+          VecIO<R>::ld(src + row * R, sv);
 #pragma unroll
-            for (int r = 0; r < R; ++r) v[r] = Pol::scale_to_b(sv[r], rb[r]);
-            VecIO<R>::st(Vj + row * R, v);
-            HT u[R];
+          for (int r = 0; r < R; ++r) v[r] = Pol::scale_to_b(sv[r], sh.rb[r]);
+          VecIO<R>::st(Vj + row * R, v);
+          HT u[R];
 #pragma unroll
-            for (int r = 0; r < R; ++r) u[r] = Pol::to_h(Pol::add_mul(Pol::mul(z[r], sc[r]), g1[r], v[r]));
-            VecIO<R>::st(H1 + row * R, u);
-          }
-        }
+          for (int r = 0; r < R; ++r) u[r] = Pol::to_h(Pol::add_mul(Pol::mul(z[r], sh.sc[r]), g1, v[r]));
+          VecIO<R>::st(H1 + row * R, u);
+        });
       }
-      if (!bar.sync()) return false;
+      ps.done();
+      if (!ps.before_next()) return false;
       for (int h = 2; h <= d; ++h) {
-        const ST gh = Pol::scalar(kp.gamma[h]);
+        const typename Pol::ST gh = Pol::scalar(kp.gamma[h]);
         const HT* hin = (h & 1) ? H0 : H1;
         HT* hout = (h & 1) ? H1 : H0;
-        for (long long s = c.gw; s < kp.nslices; s += c.tw) {
-          AT z[R];
-          spmv_slot<Pol, R, HT>(kp, s, c.lane, hin, z);
+        spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
           const long long row = slot_row(kp, s, c.lane);
-          if (row >= 0) {
-            BT v[R];
-            VecIO<R>::ld(Vj + row * R, v);
-            HT u[R];
+          if (row < 0) return;
+          BT v[R];
+          VecIO<R>::ld(Vj + row * R, v);
+          HT u[R];
 #pragma unroll
-            for (int r = 0; r < R; ++r) u[r] = Pol::to_h(Pol::add_mul(z[r], gh, v[r]));
-            VecIO<R>::st(hout + row * R, u);
-          }
-        }
-        if (!bar.sync()) return false;
+          for (int r = 0; r < R; ++r) u[r] = Pol::to_h(Pol::add_mul(z[r], gh, v[r]));
+          VecIO<R>::st(hout + row * R, u);
+        });
+        ps.done();
+        if (!ps.before_next()) return false;
       }
       // final pass: w = A u - beta_j v_{j-1}
       const HT* hin = (d & 1) ? H1 : H0;
-      for (long long s = c.gw; s < kp.nslices; s += c.tw) {
-        AT z[R];
-        spmv_slot<Pol, R, HT>(kp, s, c.lane, hin, z);
+      spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
         const long long row = slot_row(kp, s, c.lane);
-        if (row >= 0) {
-          BT v[R];
-          VecIO<R>::ld(Vj + row * R, v);
-          AT w[R];
+        if (row < 0) return;
+        BT v[R];
+        VecIO<R>::ld(Vj + row * R, v);
+        AT w[R];
 #pragma unroll
-          for (int r = 0; r < R; ++r) w[r] = z[r];
-          if (j > 0) {
-            BT vp[R];
-            VecIO<R>::ld(Vjm1 + row * R, vp);
+        for (int r = 0; r < R; ++r) w[r] = z[r];
+        if (j > 0) {
+          BT vp[R];
+          VecIO<R>::ld(Vjm1 + row * R, vp);
 #pragma unroll
-            for (int r = 0; r < R; ++r) w[r] = Pol::sub_mul(w[r], bj[r], vp[r]);
-          }
-          BT wb[R];
-#pragma unroll
-          for (int r = 0; r < R; ++r) { wb[r] = Pol::to_b(w[r]); apa[r] = Pol::dot(apa[r], w[r], v[r]); }
-          VecIO<R>::st(Wout + row * R, wb);
+          for (int r = 0; r < R; ++r) w[r] = Pol::sub_mul(w[r], sh.bj[r], vp[r]);
         }
-      }
-    }
-    double ap[R];
+        BT wb[R];
 #pragma unroll
-    for (int r = 0; r < R; ++r) ap[r] = Pol::to_d(apa[r]);
-    block_sum_store<R>(ap, part_a + c.b, G);
-    if (!bar.sync()) return false;
-    double alpha[R];
-    grid_total<R>(part_a, G, alpha);
-    // pass B: w -= alpha_j v_j; beta_{j+1} = ||w||
-    double bp[R];
+        for (int r = 0; r < R; ++r) { wb[r] = Pol::to_b(w[r]); apa[r] = Pol::dot(apa[r], w[r], v[r]); }
+        VecIO<R>::st(Wout + row * R, wb);
+      });
+    }
     {
-      ST al[R];
+      double ap[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) ap[r] = Pol::to_d(apa[r]);
+      block_sum_store<R>(ap, part_a + c.b, G);
+    }
+    ps.done();
+    if (!bar.sync()) return false;
+    grid_total_smem<R>(part_a, G, sh.alpha);
+    if (c.tid == 0) {
+      for (int r = 0; r < R; ++r) sh.al[r] = Pol::scalar(sh.alpha[r]);
+    }
+    __syncthreads();
+    // pass B: w -= alpha_j v_j; beta_{j+1} = ||w||
+    {
       AT bpa[R];
 #pragma unroll
-      for (int r = 0; r < R; ++r) { al[r] = Pol::scalar(alpha[r]); bpa[r] = Pol::zero(); }
+      for (int r = 0; r < R; ++r) bpa[r] = Pol::zero();
       for (long long i = c.gt; i < n; i += c.tt) {
         BT wb[R], v[R];
         VecIO<R>::ld(Wout + i * R, wb);
         VecIO<R>::ld(Vj + i * R, v);
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-          AT w = Pol::sub_mul(Pol::from_b(wb[r]), al[r], v[r]);
+          AT w = Pol::sub_mul(Pol::from_b(wb[r]), sh.al[r], v[r]);
           wb[r] = Pol::to_b(w);
           bpa[r] = Pol::dot_self(bpa[r], w);
         }
         VecIO<R>::st(Wout + i * R, wb);
       }
+      double bp[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) bp[r] = Pol::to_d(bpa[r]);
+      block_sum_store<R>(bp, part_b + c.b, G);
     }
-    block_sum_store<R>(bp, part_b + c.b, G);
     if (!bar.sync()) return false;
-    double tot[R];
-    grid_total<R>(part_b, G, tot);
-    bool all_broken = true;
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-      const double bn = sqrt(tot[r]);
-      if (c.b == 0 && c.tid == 0) {
-        kp.aabb[j + (long long)(m + 1) * r] = broken[r] ? 0.0 : alpha[r];
-        kp.aabb[(j + 1) + (long long)(m + 1) * (R + r)] = broken[r] ? 0.0 : bn;
-        if (!(bn == bn) || isinf(bn) || !(alpha[r] == alpha[r])) atomicCAS(kp.status, 0, (int)ST_NONFINITE);
+    grid_total_smem<R>(part_b, G, sh.tot);
+    if (c.tid == 0) {
+      int all = 1;
+      for (int r = 0; r < R; ++r) {
+        const double bn = sqrt(sh.tot[r]);
+        const double al = sh.alpha[r];
+        if (c.b == 0) {
+          kp.aabb[j + (long long)(m + 1) * r] = sh.broken[r] ? 0.0 : al;
+          kp.aabb[(j + 1) + (long long)(m + 1) * (R + r)] = sh.broken[r] ? 0.0 : bn;
+          if (!(bn == bn) || isinf(bn) || !(al == al)) atomicCAS(kp.status, 0, (int)ST_NONFINITE);
+        }
+        const double scale = fabs(al) + (j > 0 ? sh.beta[r] : 0.0);
+        if (!sh.broken[r] && j + 1 < m && !(bn > kp.bd_tol * scale)) {
+          sh.broken[r] = 1;
+          if (c.b == 0) kp.meff[r] = j + 1;
+        }
+        sh.beta[r] = sh.broken[r] ? 0.0 : bn;
+        sh.rbeta[r] = sh.broken[r] ? 0.0 : 1.0 / bn;
+        all = all && sh.broken[r];
       }
-      const double scale = fabs(alpha[r]) + (j > 0 ? beta[r] : 0.0);
-      if (!broken[r] && j + 1 < m && !(bn > kp.bd_tol * scale)) {
-        broken[r] = true;
-        if (c.b == 0 && c.tid == 0) kp.meff[r] = j + 1;
-      }
-      beta[r] = broken[r] ? 0.0 : bn;
-      rbeta[r] = broken[r] ? 0.0 : 1.0 / bn;
-      all_broken = all_broken && broken[r];
+      sh.all_broken = all;
     }
+    __syncthreads();
     src = Wout;
-    if (all_broken) break;
+    if (sh.all_broken) break;
   }
   return true;
 }
@@ -448,7 +622,7 @@ __device__ void phase_coef(const KParams& kp, const Ctx& c) {
 // X_r += sum_i A^(d-i) V_r c_{r,i}: one lift pass P_i = V c_i (V read once),
 // then d Horner passes X = A X + P_i.
 template <class Pol, int R>
-__device__ bool phase_apply(const KParams& kp, const Ctx& c, bool overwrite) {
+__device__ bool phase_apply(const KParams& kp, const Ctx& c, bool overwrite, PassSync& ps, ColStage& cs) {
   using BT = typename Pol::BT;
   using HT = typename Pol::HT;
   using AT = typename Pol::AT;
@@ -460,7 +634,10 @@ __device__ bool phase_apply(const KParams& kp, const Ctx& c, bool overwrite) {
   HT* const H0 = reinterpret_cast<HT*>(kp.H0);
   HT* const H1 = reinterpret_cast<HT*>(kp.H1);
   constexpr int IC = 3;
-  for (long long i = c.gt; i < n; i += c.tt) {
+  const long long sb = kp.blk_slice[c.b], se = kp.blk_slice[c.b + 1];
+  for (long long s = sb + c.warp; s < se; s += c.nw) {
+    const long long i = slot_row(kp, s, c.lane);
+    if (i < 0) continue;
     for (int i0 = 0; i0 < d1; i0 += IC) {
       AT acc[IC][R];
 #pragma unroll
@@ -513,43 +690,44 @@ __device__ bool phase_apply(const KParams& kp, const Ctx& c, bool overwrite) {
     }
   }
   if (d == 0) return true;
-  if (!bar.sync()) return false;
+  ps.done();
+  if (!ps.before_next()) return false;
   for (int h = 1; h <= d; ++h) {
     const HT* hin = h == 1 ? P : ((h & 1) ? H0 : H1);
     HT* hout = (h & 1) ? H1 : H0;
     const HT* Ph = P + (long long)h * n * R;
-    for (long long s = c.gw; s < kp.nslices; s += c.tw) {
-      AT z[R];
-      spmv_slot<Pol, R, HT>(kp, s, c.lane, hin, z);
+    spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
       const long long row = slot_row(kp, s, c.lane);
-      if (row >= 0) {
-        HT p[R];
-        VecIO<R>::ld(Ph + row * R, p);
-        AT x[R];
+      if (row < 0) return;
+      HT p[R];
+      VecIO<R>::ld(Ph + row * R, p);
+      AT x[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) x[r] = Pol::add(z[r], h_load_at<Pol>(p[r]));
-        if (h < d) {
-          HT hv[R];
+      for (int r = 0; r < R; ++r) x[r] = Pol::add(z[r], h_load_at<Pol>(p[r]));
+      if (h < d) {
+        HT hv[R];
 #pragma unroll
-          for (int r = 0; r < R; ++r) hv[r] = Pol::to_h(x[r]);
-          VecIO<R>::st(hout + row * R, hv);
+        for (int r = 0; r < R; ++r) hv[r] = Pol::to_h(x[r]);
+        VecIO<R>::st(hout + row * R, hv);
+      } else {
+        double xo[R], u[R], so[R];
+        if (overwrite) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) xo[r] = 0.0;
         } else {
-          double xo[R], u[R], so[R];
-          if (overwrite) {
-#pragma unroll
-            for (int r = 0; r < R; ++r) xo[r] = 0.0;
-          } else {
-            VecIO<R>::ld(kp.X + row * R, xo);
-          }
-          VecIO<R>::ld(kp.upd + row * R, u);
-#pragma unroll
-          for (int r = 0; r < R; ++r) { xo[r] += Pol::to_d(x[r]); so[r] = xo[r] + u[r]; }
-          VecIO<R>::st(kp.X + row * R, xo);
-          VecIO<R>::st(kp.S + row * R, so);
+          VecIO<R>::ld(kp.X + row * R, xo);
         }
+        VecIO<R>::ld(kp.upd + row * R, u);
+#pragma unroll
+        for (int r = 0; r < R; ++r) { xo[r] += Pol::to_d(x[r]); so[r] = xo[r] + u[r]; }
+        VecIO<R>::st(kp.X + row * R, xo);
+        VecIO<R>::st(kp.S + row * R, so);
       }
+    });
+    if (h < d) {
+      ps.done();
+      if (!ps.before_next()) return false;
     }
-    if (h < d && !bar.sync()) return false;
   }
   return true;
 }
@@ -672,12 +850,18 @@ __device__ bool phase_deflate(const KParams& kp, const Ctx& c, int mode) {
 // PH is the compile-time set of phases this entry point can run (the runtime
 // mask kp.phases selects among them); specialising on it lets the compiler
 // size registers per phase group.
+#ifndef GM_MINB
+#define GM_MINB 2
+#endif
 template <class Pol, int R, int PH>
-__global__ void __launch_bounds__(512, (R >= 4 ? 1 : 2)) fab_kernel(KParams kp) {
+__global__ void __launch_bounds__(512, (R >= 4 ? 1 : GM_MINB)) fab_kernel(KParams kp) {
   const Ctx c(kp.G);
   GridBar bar{kp.bar, kp.bar + 1, kp.status, (unsigned)kp.G, kp.timeout_ns};
   if (*(volatile int*)kp.status != 0) return;
   const int ph = kp.phases & PH;
+  PassSync ps{bar, make_dep(kp), kp.dep_mode, 0u};
+  ColStage cs;
+  if (PH & (PH_LANCZOS | PH_APPLY)) cs.init(kp, c);
   bool first = true;
   auto sep = [&]() -> bool {
     if (first) { first = false; return true; }
@@ -685,7 +869,7 @@ __global__ void __launch_bounds__(512, (R >= 4 ? 1 : 2)) fab_kernel(KParams kp) 
   };
   if ((PH & PH_LANCZOS) && (ph & PH_LANCZOS)) {
     if (!sep()) return;
-    if (!phase_lanczos<Pol, R>(kp, c)) return;
+    if (!phase_lanczos<Pol, R>(kp, c, ps, cs)) return;
   }
   if ((PH & PH_TRISOLVE) && (ph & PH_TRISOLVE)) {
     if (!sep()) return;
@@ -697,7 +881,7 @@ __global__ void __launch_bounds__(512, (R >= 4 ? 1 : 2)) fab_kernel(KParams kp) 
   }
   if ((PH & PH_APPLY) && (ph & PH_APPLY)) {
     if (!sep()) return;
-    if (!phase_apply<Pol, R>(kp, c, (ph & PH_APPLY_SET) != 0)) return;
+    if (!phase_apply<Pol, R>(kp, c, (ph & PH_APPLY_SET) != 0, ps, cs)) return;
   }
   if (PH & (PH_DEFLATE | PH_UPDATE_FKPP | PH_UPDATE_FHN)) {
     const int upd_mode = (ph & PH_UPDATE_FKPP) ? 1 : ((ph & PH_UPDATE_FHN) ? 2 : 0);

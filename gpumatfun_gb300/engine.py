@@ -58,6 +58,7 @@ class CreateArgs(ct.Structure):
         ("precision", ct.c_int), ("sync_mode", ct.c_int), ("threads_per_block", ct.c_int),
         ("blocks_per_sm", ct.c_int), ("sell_sigma", ct.c_int),
         ("barrier_timeout_s", ct.c_double), ("breakdown_tol", ct.c_double),
+        ("sync_policy", ct.c_int), ("col_staging", ct.c_int),
     ]
 
 
@@ -122,7 +123,8 @@ class Engine:
                  dt: float = 1.0, col_scale=None, mass=None, ode=None, fhn: dict | None = None,
                  precision: str | int = "fp64", sync: bool = True, threads: int = 0,
                  blocks_per_sm: int = 0, sell_sigma: int = 0, timeout_s: float = 0.0,
-                 breakdown_tol: float = 0.0, matrix_format: str = "csr"):
+                 breakdown_tol: float = 0.0, matrix_format: str = "csr", sync_policy: int = 0,
+                 col_staging: int = 0):
         self._lib = load_library()
         self._h = ct.c_void_p()
         n = A.shape[0]
@@ -174,6 +176,8 @@ class Engine:
         a.precision, a.sync_mode = int(prec), 1 if sync else 0
         a.threads_per_block, a.blocks_per_sm, a.sell_sigma = threads, blocks_per_sm, sell_sigma
         a.barrier_timeout_s, a.breakdown_tol = timeout_s, breakdown_tol
+        a.sync_policy = int(sync_policy)
+        a.col_staging = int(col_staging)
         self._keep = (ptr, ind, val, U, Q, lam, flam, gamma, gs_re, gs_im, wts, shifts, cs, mass, ode)
         rc = self._lib.gm_lanczos_create(ct.byref(a), ct.byref(self._h))
         self._keep = None

@@ -105,6 +105,11 @@ typedef struct gm_create_args {
   int sell_sigma;              /* SELL-32 sorting window in rows; 0/1 = unsorted  */
   double barrier_timeout_s;    /* 0 = 5 s                                         */
   double breakdown_tol;        /* 0 = 64 eps, relative to |alpha_j| + beta_j      */
+  int sync_policy;             /* ordering of consecutive SpMV passes: 0 = waits on
+                                  the blocks owning referenced rows (default),
+                                  1 = grid barriers                               */
+  int col_staging;             /* 0 = stage SELL column indices in shared memory by
+                                  TMA bulk copies (default), 1 = read them directly */
 } gm_create_args;
 
 /* Fill *args with defaults (zeros, struct_version, sync_mode = 1, nrhs = 2). */

@@ -259,6 +259,32 @@ def test_zero_rhs(engine_lib):
     assert np.all(eng.get_solution() == 0.0)
 
 
+@pytest.mark.parametrize("degree", [0, 3, 6])
+def test_sync_policies_agree(engine_lib, degree):
+    """Neighbour waits between SpMV passes (default) and grid barriers give
+    the same bits: the passes compute identical values in identical order.
+    The grid is large (hundreds of blocks, several Horner passes in both the
+    Lanczos and the apply phase) so that an ordering race would show."""
+    N = 180
+    P = workloads.fd2d_problem(N, 3, 24, 24, [params.frac_exp(1e-3, 1.5)] * 2, R=2, scale=(N + 1.0) ** 2,
+                               seed=2, degree=degree)
+    want = oracle_for(P).solve()
+    out = []
+    for pol in (0, 1):
+        eng = Engine.from_problem(P, sync_policy=pol, threads=128, sync=False)
+        assert eng.info()["grid_blocks"] > 200
+        for _ in range(3):
+            eng.solve()
+            out.append(eng.get_solution())
+        eng.set_U(P.U)  # X = 0 again: apply_V accumulates
+        eng.build_subspace(); eng.lin_sys_solves(); eng.apply_V()
+        out.append(eng.get_solution())
+        eng.delete()
+    for x in out[1:]:
+        np.testing.assert_array_equal(x, out[0])
+    assert rel(out[0], want) < FP64_TOL
+
+
 def test_no_deflation_and_sigma_sorted(engine_lib):
     P = workloads.fd2d_problem(20, 0, 40, 24, [params.frac_exp(1e-3, 1.5)], R=1, scale=441.0, seed=8)
     ora = oracle_for(P)
