@@ -175,7 +175,7 @@ def run_reference(args, P, rank):
 def config_of(args, P):
     return {"workload": P.name, "n": int(P.n), "nnz": int(P.A.nnz), "m": int(P.m), "C": int(P.C),
             "d": int(P.d), "k": int(P.k), "nrhs": int(args.nrhs), "precision": args.precision,
-            "f": "x^-0.8" if "disk" in P.name else "exp(-tau x^(alpha/2))",
+            "f": P.meta.get("f", "x^-0.8" if "disk" in P.name else "exp(-tau x^(alpha/2))"),
             "l2": "inputs larger than L2 (Krylov basis m x n x 8 B per RHS)",
             "parallelism": f"replicas x{args.gpus}"}
 
@@ -292,28 +292,40 @@ def run_ours(args, P, rank, world, local):
     torch.cuda.empty_cache()
 
     if rank == 0 and not args.no_extras:
-        line["accuracy"] = accuracy_checks(P, x_last, B_last=None)
-        line["mixed_batched"] = mixed_batched(P, K, W, dev, stream, x_ref_engine=None)
+        line["accuracy"] = accuracy_checks(P, args.precision)
+        if args.precision == "fp64":
+            line["mixed_batched"] = mixed_batched(P, K, W, dev, stream, x_ref_engine=None)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(P, host_deflate(P, P.U), args.cpu_sample_s, 0)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
 
-def accuracy_checks(P, x_last, B_last):
-    """FP64 engine vs the FP64 oracle on the workload's own b (one solve)."""
+def accuracy_checks(P, precision):
+    """On the workload's own b: the FP64 engine against the FP64 oracle (when
+    the oracle is affordable, n <= 2M) and, for the mixed engine, the mixed
+    result against the FP64 engine run."""
     from gpumatfun_gb300 import Engine
-    from oracle import fab
+    out = {}
     eng = Engine.from_problem(P, precision="fp64")
     eng.solve()
     x = eng.get_solution()
     eng.delete()
-    t0 = time.perf_counter()
-    ora = fab.OracleEngine(A=P.A, U0=P.U, Q=P.Q, m=P.m, gamma=P.gamma, gs_re=P.gs_re, gs_im=P.gs_im,
-                           flam=P.flam, wts=P.wts, shifts=P.shifts, col_scale=np.ones(P.R))
-    want = ora.solve()
-    return {"fp64_vs_oracle_rel_err": float(np.linalg.norm(x - want) / np.linalg.norm(want)),
-            "oracle_s": time.perf_counter() - t0}
+    if precision == "mixed":
+        em = Engine.from_problem(P, precision="mixed")
+        em.solve()
+        xm = em.get_solution()
+        em.delete()
+        out["mixed_vs_fp64_engine_rel_err"] = float(np.linalg.norm(xm - x) / np.linalg.norm(x))
+    if P.n <= 2_000_000:
+        from oracle import fab
+        t0 = time.perf_counter()
+        ora = fab.OracleEngine(A=P.A, U0=P.U, Q=P.Q, m=P.m, gamma=P.gamma, gs_re=P.gs_re, gs_im=P.gs_im,
+                               flam=P.flam, wts=P.wts, shifts=P.shifts, col_scale=np.ones(P.R))
+        want = ora.solve()
+        out["fp64_vs_oracle_rel_err"] = float(np.linalg.norm(x - want) / np.linalg.norm(want))
+        out["oracle_s"] = time.perf_counter() - t0
+    return out
 
 
 def mixed_batched(P, K, W, dev, stream, x_ref_engine=None):

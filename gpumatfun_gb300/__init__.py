@@ -1,7 +1,7 @@
 """GB300-native f(A)b engine (polynomial-preconditioned Lanczos, deflation and
 contour-integral evaluation of f on the tridiagonal), with the reference's
 handle API (``LanczosEngine``) over a C ABI (include/gpumatfun.h)."""
-from .engine import Engine, LanczosEngine, GmError, load_library  # noqa: F401
+from .engine import Engine, LanczosEngine, BatchEngine, GmError, load_library  # noqa: F401
 from . import params, problems, workloads  # noqa: F401
 
 __version__ = "0.1.0"

@@ -1,0 +1,109 @@
+"""Autotuner for the engine's launch shape.
+
+Times candidate launch shapes of the fused solve on the actual workload and
+keeps the fastest.  The knobs are the ones the engine exposes at create time:
+- threads per block (the row-block size: 32 SELL rows per warp);
+- resident blocks per SM;
+- TMA staging of SELL column indices on or off;
+- neighbour waits vs grid barriers between SpMV passes.
+
+Results are cached in a JSON file keyed by a signature of the workload:
+- n, nnz, a row-length histogram and the number of right-hand sides;
+- m, d, C and precision;
+- the device name.
+
+A repeated workload therefore reuses the tuned shape without timing again.
+"""
+from __future__ import annotations
+
+import hashlib
+import itertools
+import json
+import os
+from typing import Callable
+
+import numpy as np
+
+__all__ = ["signature", "candidates", "tune", "default_cache_path"]
+
+
+def default_cache_path() -> str:
+    base = os.environ.get("GPUMATFUN_CACHE") or os.path.join(os.environ.get("TMPDIR", "/tmp"), "gpumatfun_cache")
+    return os.path.join(base, "autotune.json")
+
+
+def signature(P, precision: str, device: str = "") -> str:
+    """Stable key of the quantities that decide the best launch shape."""
+    lens = np.diff(P.A.indptr)
+    hist = np.bincount(np.minimum(lens, 32), minlength=33)
+    frac = np.round(hist / max(1, lens.size), 3).tolist()
+    key = dict(n=int(P.n), nnz=int(P.A.nnz), rowlen=frac, R=int(P.R), m=int(P.m), d=int(P.d), C=int(P.C),
+               precision=str(precision), device=device)
+    return hashlib.sha1(json.dumps(key, sort_keys=True).encode()).hexdigest()[:16]
+
+
+def candidates(R: int) -> list:
+    """The search space (row-block sizes, residency, staging, pass ordering)."""
+    threads = (128, 256, 512)
+    bps = (0, 1) if R >= 4 else (0, 1, 2)
+    out = []
+    for t, b, stg, pol in itertools.product(threads, bps, (0, 1), (0, 1)):
+        out.append(dict(threads=t, blocks_per_sm=b, col_staging=stg, sync_policy=pol))
+    return out
+
+
+def _measure_engine(P, precision: str, reps: int) -> Callable[[dict], float]:
+    from .engine import Engine, GmError
+
+    def run(cand: dict) -> float:
+        try:
+            eng = Engine.from_problem(P, precision=precision, sync=False, **cand)
+        except GmError:
+            return float("inf")
+        try:
+            eng.solve()
+            eng.sync()
+            ts = []
+            for _ in range(reps):
+                eng.solve()
+                ts.append(eng.phase_times()["solve"])
+            return float(np.median(ts))
+        finally:
+            eng.delete()
+    return run
+
+
+def tune(P, precision: str = "fp64", reps: int = 3, cache_path: str | None = None,
+         space: list | None = None, measure: Callable[[dict], float] | None = None,
+         device: str = "", force: bool = False) -> dict:
+    """Best launch shape for workload P: a dict of Engine keyword arguments
+    plus 'ms' (median fused-solve time).  ``measure`` replaces the GPU timing
+    (tests); ``space`` replaces the candidate list."""
+    cache_path = cache_path or default_cache_path()
+    key = signature(P, precision, device)
+    cache = {}
+    if os.path.exists(cache_path):
+        try:
+            with open(cache_path) as fh:
+                cache = json.load(fh)
+        except (OSError, ValueError):
+            cache = {}
+    if not force and key in cache:
+        return dict(cache[key], cached=True)
+    measure = measure or _measure_engine(P, precision, reps)
+    best, best_ms, trials = None, float("inf"), []
+    for cand in (space or candidates(P.R)):
+        ms = measure(cand)
+        trials.append(dict(cand, ms=ms))
+        if ms < best_ms:
+            best, best_ms = cand, ms
+    if best is None:
+        raise RuntimeError("autotune: no candidate ran")
+    result = dict(best, ms=best_ms, trials=len(trials))
+    cache[key] = result
+    os.makedirs(os.path.dirname(cache_path) or ".", exist_ok=True)
+    tmp = f"{cache_path}.tmp{os.getpid()}"
+    with open(tmp, "w") as fh:
+        json.dump(cache, fh, indent=1)
+    os.replace(tmp, cache_path)
+    return dict(result, cached=False)

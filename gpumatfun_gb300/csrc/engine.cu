@@ -39,7 +39,7 @@ struct gm_engine {
   cudaStream_t own_stream = nullptr;
   cudaStream_t stream = nullptr;
   long long n = 0, nnz = 0, nslices = 0, padded = 0;
-  int R = 0, m = 0, d = 0, C = 0, k = 0, prec = 0, sync_mode = 1;
+  int R = 0, m = 0, d = 0, C = 0, k = 0, prec = 0, sync_mode = 1, nprob = 1;
   int threads = 512, G = 0;
   int scale_exp = 0;             // mixed engine: A stored as A * 2^-scale_exp
   unsigned long long epoch = 0;  // launch counter (progress-flag epochs)
@@ -56,6 +56,9 @@ struct gm_engine {
   cudaEvent_t ev[5][2] = {};
   bool ev_used[5] = {};
   bool have_y = false, have_coef = false, have_V = false;
+  bool capturing = false;        // launches are being recorded into a CUDA graph
+  cudaGraphExec_t loop_exec = nullptr;
+  int loop_steps = -1, loop_mode = -1;
   long long launches = 0;
   std::string err;
 };
@@ -130,24 +133,39 @@ struct Csr {
   std::vector<double> val;
 };
 
-int make_csr(gm_engine* e, const gm_create_args* a, Csr& out) {
-  const long long n = a->n;
-  const long long* ptr = reinterpret_cast<const long long*>(a->ptr);
-  const long long* ind = reinterpret_cast<const long long*>(a->ind);
+// One problem's matrix as given (CSC as MATLAB stores it, or CSR) -> CSR.
+struct ProbIn {
+  long long n, nnz_hint;
+  int format;
+  const long long* ptr;
+  const long long* ind;
+  const double* values;
+  const double* U;
+  const double* gamma;
+  const double* gs_re;
+  const double* gs_im;
+  const double* wts;
+  const double* shifts;
+};
+
+int make_csr(gm_engine* e, const ProbIn& a, Csr& out) {
+  const long long n = a.n;
+  const long long* ptr = a.ptr;
+  const long long* ind = a.ind;
   if (ptr[0] != 0) return fail(e, GM_ERR_ARG, "lanczos_create:inputNotSparse: pointer array must start at 0");
   for (long long i = 0; i < n; ++i)
     if (ptr[i + 1] < ptr[i]) return fail(e, GM_ERR_ARG, "lanczos_create:inputNotSparse: pointer array not monotone at %lld", i);
   const long long nnz = ptr[n];
-  if (a->nnz && a->nnz < nnz) return fail(e, GM_ERR_ARG, "lanczos_create:inputNotSparse: nnz %lld < ptr[n] %lld", (long long)a->nnz, nnz);
+  if (a.nnz_hint && a.nnz_hint < nnz) return fail(e, GM_ERR_ARG, "lanczos_create:inputNotSparse: nnz %lld < ptr[n] %lld", a.nnz_hint, nnz);
   if (nnz > 2147483647LL) return fail(e, GM_ERR_UNSUPPORTED, "more than 2^31-1 stored entries");
   for (long long t = 0; t < nnz; ++t)
     if (ind[t] < 0 || ind[t] >= n) return fail(e, GM_ERR_ARG, "lanczos_create:inputNotSparse: index %lld out of range at %lld", (long long)ind[t], t);
   out.ptr.assign(n + 1, 0);
   out.col.resize(nnz);
   out.val.resize(nnz);
-  if (a->format == GM_CSR) {
+  if (a.format == GM_CSR) {
     for (long long i = 0; i <= n; ++i) out.ptr[i] = ptr[i];
-    for (long long t = 0; t < nnz; ++t) { out.col[t] = (int)ind[t]; out.val[t] = a->values[t]; }
+    for (long long t = 0; t < nnz; ++t) { out.col[t] = (int)ind[t]; out.val[t] = a.values[t]; }
   } else {
     // CSC of A -> CSR of A (counting sort by row).  The reference uploads the
     // CSC arrays as the CSR of A^T and multiplies with the transpose flag
@@ -161,27 +179,43 @@ int make_csr(gm_engine* e, const gm_create_args* a, Csr& out) {
       for (long long t = ptr[j]; t < ptr[j + 1]; ++t) {
         const long long p = pos[ind[t]]++;
         out.col[p] = (int)j;
-        out.val[p] = a->values[t];
+        out.val[p] = a.values[t];
       }
   }
-  e->nnz = nnz;
   return GM_OK;
 }
 
+// Appends B (rows and columns shifted by row0) to the block-diagonal A.
+void append_block(Csr& A, const Csr& B, long long row0) {
+  const long long base = A.ptr.empty() ? 0 : A.ptr.back();
+  if (A.ptr.empty()) A.ptr.push_back(0);
+  for (size_t i = 1; i < B.ptr.size(); ++i) A.ptr.push_back(base + B.ptr[i]);
+  for (int c : B.col) A.col.push_back((int)(c + row0));
+  A.val.insert(A.val.end(), B.val.begin(), B.val.end());
+}
+
+// SELL-32 over the block-diagonal matrix: every problem starts on a new
+// slice, so a slice never mixes problems (pad slots map to row -1).
 template <class VT>
-int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp, std::vector<long long>& rows,
-                std::vector<long long>& off) {
-  const long long n = e->n;
-  const long long nsl = (n + 31) / 32;
-  bool sorted = sigma > 1;
+int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp, const std::vector<long long>& prow0,
+                std::vector<long long>& rows, std::vector<long long>& off, std::vector<long long>& pslice0) {
+  const int np = (int)prow0.size() - 1;
+  pslice0.assign(np + 1, 0);
+  for (int p = 0; p < np; ++p) pslice0[p + 1] = pslice0[p] + (prow0[p + 1] - prow0[p] + 31) / 32;
+  const long long nsl = pslice0[np];
+  const bool sorted = sigma > 1;
   rows.assign(nsl * 32, -1);
-  for (long long s = 0; s < nsl * 32; ++s) rows[s] = s < n ? s : -1;
-  if (sorted) {
-    for (long long w0 = 0; w0 < n; w0 += sigma) {
-      const long long w1 = std::min<long long>(n, w0 + sigma);
-      std::stable_sort(rows.begin() + w0, rows.begin() + w1, [&](long long x, long long y) {
-        return (A.ptr[x + 1] - A.ptr[x]) > (A.ptr[y + 1] - A.ptr[y]);
-      });
+  for (int p = 0; p < np; ++p) {
+    const long long n_p = prow0[p + 1] - prow0[p];
+    long long* rp = rows.data() + pslice0[p] * 32;
+    for (long long i = 0; i < n_p; ++i) rp[i] = prow0[p] + i;
+    if (sorted) {
+      for (long long w0 = 0; w0 < n_p; w0 += sigma) {
+        const long long w1 = std::min<long long>(n_p, w0 + sigma);
+        std::stable_sort(rp + w0, rp + w1, [&](long long x, long long y) {
+          return (A.ptr[x + 1] - A.ptr[x]) > (A.ptr[y + 1] - A.ptr[y]);
+        });
+      }
     }
   }
   off.assign(nsl + 1, 0);
@@ -225,7 +259,7 @@ int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp, std::vecto
   e->kp.col = d_col;
   e->kp.val = d_val;
   e->kp.perm = nullptr;
-  if (sorted) {
+  if (sorted || np > 1) {
     std::vector<int> p32(rows.size());
     for (size_t s = 0; s < rows.size(); ++s) p32[s] = (int)rows[s];
     int* d_perm;
@@ -243,20 +277,47 @@ int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp, std::vecto
 // list of other blocks owning a row that one of its rows references, closed
 // under symmetry (see DepSync in fab_common.cuh).
 int build_partition(gm_engine* e, const Csr& A, const std::vector<long long>& rows,
-                    const std::vector<long long>& off) {
-  const long long nsl = (long long)off.size() - 1;
-  const int G = e->G;
-  std::vector<int> bs(G + 1, 0);
-  double total = 0.0;
-  for (long long s = 0; s < nsl; ++s) total += (double)(off[s + 1] - off[s]) + 32.0 * 4.0;
-  double acc = 0.0;
-  int b = 0;
-  for (long long s = 0; s < nsl; ++s) {
-    const double w = (double)(off[s + 1] - off[s]) + 32.0 * 4.0;
-    while (b < G - 1 && acc + 0.5 * w > total * (b + 1) / G) bs[++b] = (int)s;
-    acc += w;
+                    const std::vector<long long>& off, const std::vector<long long>& pslice0,
+                    const std::vector<long long>& prow0) {
+  const int np = (int)pslice0.size() - 1;
+  // blocks per problem in proportion to its work, at least one, at most one
+  // per slice; e->G becomes the total
+  std::vector<double> work(np, 0.0);
+  std::vector<int> gp(np, 1);
+  for (int p = 0; p < np; ++p)
+    for (long long s = pslice0[p]; s < pslice0[p + 1]; ++s) work[p] += (double)(off[s + 1] - off[s]) + 32.0 * 4.0;
+  if (e->G < np) return fail(e, GM_ERR_UNSUPPORTED, "%d problems need at least as many resident blocks (have %d)", np, e->G);
+  for (int extra = e->G - np; extra > 0; --extra) {
+    int best = -1;
+    double bw = -1.0;
+    for (int p = 0; p < np; ++p)
+      if (gp[p] < pslice0[p + 1] - pslice0[p] && work[p] / gp[p] > bw) { bw = work[p] / gp[p]; best = p; }
+    if (best < 0) break;
+    gp[best]++;
   }
-  while (b < G) bs[++b] = (int)nsl;
+  std::vector<int> pb0(np + 1, 0);
+  for (int p = 0; p < np; ++p) pb0[p + 1] = pb0[p] + gp[p];
+  const int G = pb0[np];
+  e->G = G;
+  for (int g = 0; g < 5; ++g) e->Gk[g] = G;
+  e->kp.G = G;
+  std::vector<int> bs(G + 1, 0), bprob(G, 0);
+  for (int p = 0; p < np; ++p) {
+    double total = 0.0;
+    for (long long s = pslice0[p]; s < pslice0[p + 1]; ++s) total += (double)(off[s + 1] - off[s]) + 32.0 * 4.0;
+    double acc = 0.0;
+    int b = 0;
+    const int Gp = gp[p];
+    bs[pb0[p]] = (int)pslice0[p];
+    for (long long s = pslice0[p]; s < pslice0[p + 1]; ++s) {
+      const double w = (double)(off[s + 1] - off[s]) + 32.0 * 4.0;
+      while (b < Gp - 1 && acc + 0.5 * w > total * (b + 1) / Gp) bs[pb0[p] + (++b)] = (int)s;
+      acc += w;
+    }
+    while (b < Gp - 1) bs[pb0[p] + (++b)] = (int)pslice0[p + 1];
+    bs[pb0[p + 1]] = (int)pslice0[p + 1];
+    for (int q = pb0[p]; q < pb0[p + 1]; ++q) bprob[q] = p;
+  }
   std::vector<int> owner(e->n, 0);
   for (int q = 0; q < G; ++q)
     for (long long s = bs[q]; s < bs[q + 1]; ++s)
@@ -288,8 +349,18 @@ int build_partition(gm_engine* e, const Csr& A, const std::vector<long long>& ro
   int* d_bs;
   int* d_dp;
   int* d_di;
+  int* d_bprob;
+  int* d_pb0;
+  long long* d_prow0;
   unsigned long long* d_prog;
   int rc;
+  if ((rc = dupload(e, &d_bprob, bprob.data(), bprob.size()))) return rc;
+  if ((rc = dupload(e, &d_pb0, pb0.data(), pb0.size()))) return rc;
+  if ((rc = dupload(e, &d_prow0, prow0.data(), prow0.size()))) return rc;
+  e->kp.nprob = np;
+  e->kp.blk_prob = d_bprob;
+  e->kp.prob_blk0 = d_pb0;
+  e->kp.prob_row0 = d_prow0;
   if ((rc = dupload(e, &d_bs, bs.data(), bs.size()))) return rc;
   if ((rc = dupload(e, &d_dp, dp.data(), dp.size()))) return rc;
   if ((rc = dupload(e, &d_di, di.data(), di.size()))) return rc;
@@ -332,7 +403,7 @@ int map_status(gm_engine* e, int st) {
 
 int check_sync(gm_engine* e) {
   GM_CUDA(e, cudaMemcpyAsync(e->h_status, e->kp.status, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
-  GM_CUDA(e, cudaMemcpyAsync(e->h_status + 1, e->kp.meff, sizeof(int) * e->R, cudaMemcpyDeviceToHost, e->stream));
+  GM_CUDA(e, cudaMemcpyAsync(e->h_status + 1, e->kp.meff, sizeof(int) * e->R * e->nprob, cudaMemcpyDeviceToHost, e->stream));
   GM_CUDA(e, cudaStreamSynchronize(e->stream));
   return map_status(e, e->h_status[0]);
 }
@@ -345,15 +416,33 @@ int launch(gm_engine* e, int phases, int slot) {
   KParams kp = e->kp;
   kp.phases = phases;
   void* args[] = {&kp};
-  GM_CUDA(e, cudaEventRecord(e->ev[slot][0], e->stream));
   const int grp = group_of(phases);
   kp.G = e->Gk[grp];
-  kp.epoch = ++e->epoch;
-  cudaError_t st = cudaLaunchCooperativeKernel(e->kfn[grp], dim3(kp.G), dim3(e->threads), args, e->smem[grp], e->stream);
-  if (st != cudaSuccess) return cuda_fail(e, st, "cudaLaunchCooperativeKernel");
+  if (e->capturing) {
+    // A captured launch replays with the same parameters, so the progress
+    // flags are cleared by a memset node before it and a fixed epoch is used.
+    GM_CUDA(e, cudaMemsetAsync(e->kp.prog, 0, sizeof(unsigned long long) * e->G, e->stream));
+    kp.epoch = 1;
+  } else {
+    GM_CUDA(e, cudaEventRecord(e->ev[slot][0], e->stream));
+    kp.epoch = ++e->epoch;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kp.G);
+  cfg.blockDim = dim3(e->threads);
+  cfg.dynamicSmemBytes = e->smem[grp];
+  cfg.stream = e->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaError_t st = cudaLaunchKernelExC(&cfg, e->kfn[grp], args);
+  if (st != cudaSuccess) return cuda_fail(e, st, "cooperative launch");
+  e->launches++;
+  if (e->capturing) return GM_OK;
   GM_CUDA(e, cudaEventRecord(e->ev[slot][1], e->stream));
   e->ev_used[slot] = true;
-  e->launches++;
   if (e->sync_mode) return check_sync(e);
   return GM_OK;
 }
@@ -391,6 +480,7 @@ int set_usol(gm_engine* e, const double* U, bool on_device) {
 void destroy(gm_engine* e) {
   if (!e) return;
   if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->loop_exec) cudaGraphExecDestroy(e->loop_exec);
   for (auto& b : e->bufs) cudaFree(b.p);
   e->bufs.clear();
   for (int s = 0; s < 5; ++s)
@@ -401,26 +491,37 @@ void destroy(gm_engine* e) {
   delete e;
 }
 
-int create_impl(const gm_create_args* a, gm_engine* e) {
+// Creates the engine for one problem (gm_lanczos_create) or several
+// independent problems sharing m, C, d and nrhs (gm_batch_create).
+int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_engine* e) {
   if (a->struct_version != GM_CREATE_ARGS_VERSION)
     return fail(e, GM_ERR_ARG, "lanczos_create:invalidNumInputs: struct_version %d != %d", a->struct_version, GM_CREATE_ARGS_VERSION);
-  if (a->n <= 0) return fail(e, GM_ERR_ARG, "lanczos_create:inputNotSquare: n must be positive");
-  if (!a->ptr || (!a->ind && a->n > 0) || !a->values) return fail(e, GM_ERR_ARG, "lanczos_create:inputNotSparse: null sparse array");
-  if (a->format != GM_CSC && a->format != GM_CSR) return fail(e, GM_ERR_ARG, "unknown matrix format %d", a->format);
+  const int np = (int)probs.size();
+  if (np < 1) return fail(e, GM_ERR_ARG, "batch_create: no problems");
   if (a->nrhs != 1 && a->nrhs != 2 && a->nrhs != 4) return fail(e, GM_ERR_ARG, "lanczos_create:badU: nrhs must be 1, 2 or 4 (got %d)", a->nrhs);
-  if (!a->U) return fail(e, GM_ERR_ARG, "lanczos_create:badU: null U");
   if (a->num_eigs < 0 || (a->num_eigs > 0 && (!a->Q || !a->flam)))
     return fail(e, GM_ERR_ARG, "lanczos_create:badQ: num_eigs %d needs Q and f(lambda)", a->num_eigs);
+  if (np > 1 && a->num_eigs > 0) return fail(e, GM_ERR_UNSUPPORTED, "batch_create: deflation needs a single problem");
   if (a->subspace_size < 1) return fail(e, GM_ERR_ARG, "lanczos_create:bad_N: subspace size must be >= 1");
-  if (a->gamma_size < 1 || !a->gamma) return fail(e, GM_ERR_ARG, "lanczos_create:bad_gamma: gamma_size must be >= 1");
-  if (a->contour_size < 1 || !a->gamma_s_real || !a->gamma_s_imag)
-    return fail(e, GM_ERR_ARG, "lanczos_create:bad_gamma_s_real: contour size must be >= 1");
-  if (!a->wts) return fail(e, GM_ERR_ARG, "lanczos_create:bad_wts1: null weights");
-  if (!a->shifts) return fail(e, GM_ERR_ARG, "lanczos_create:bad_shifts: null shifts");
+  if (a->gamma_size < 1) return fail(e, GM_ERR_ARG, "lanczos_create:bad_gamma: gamma_size must be >= 1");
+  if (a->contour_size < 1) return fail(e, GM_ERR_ARG, "lanczos_create:bad_gamma_s_real: contour size must be >= 1");
   if (a->precision != GM_FP64 && a->precision != GM_MIXED) return fail(e, GM_ERR_ARG, "unknown precision %d", a->precision);
-  if (a->n > 2147483647LL) return fail(e, GM_ERR_UNSUPPORTED, "n above 2^31-1");
+  long long ntot = 0;
+  for (int p = 0; p < np; ++p) {
+    const ProbIn& q = probs[p];
+    if (q.n <= 0) return fail(e, GM_ERR_ARG, "lanczos_create:inputNotSquare: n must be positive (problem %d)", p);
+    if (!q.ptr || !q.ind || !q.values) return fail(e, GM_ERR_ARG, "lanczos_create:inputNotSparse: null sparse array (problem %d)", p);
+    if (q.format != GM_CSC && q.format != GM_CSR) return fail(e, GM_ERR_ARG, "unknown matrix format %d", q.format);
+    if (!q.U) return fail(e, GM_ERR_ARG, "lanczos_create:badU: null U (problem %d)", p);
+    if (!q.gamma) return fail(e, GM_ERR_ARG, "lanczos_create:bad_gamma: null gamma (problem %d)", p);
+    if (!q.gs_re || !q.gs_im) return fail(e, GM_ERR_ARG, "lanczos_create:bad_gamma_s_real: null shifted coefficients (problem %d)", p);
+    if (!q.wts) return fail(e, GM_ERR_ARG, "lanczos_create:bad_wts1: null weights (problem %d)", p);
+    if (!q.shifts) return fail(e, GM_ERR_ARG, "lanczos_create:bad_shifts: null shifts (problem %d)", p);
+    ntot += q.n;
+  }
+  if (ntot > 2147483647LL) return fail(e, GM_ERR_UNSUPPORTED, "n above 2^31-1");
 
-  e->n = a->n; e->R = a->nrhs; e->m = a->subspace_size; e->d = a->gamma_size - 1;
+  e->n = ntot; e->nprob = np; e->R = a->nrhs; e->m = a->subspace_size; e->d = a->gamma_size - 1;
   e->C = a->contour_size; e->k = a->num_eigs; e->prec = a->precision; e->sync_mode = a->sync_mode;
   e->threads = a->threads_per_block ? a->threads_per_block : 512;
   if (e->threads % 32 || e->threads < 64 || e->threads > 512)
@@ -434,11 +535,19 @@ int create_impl(const gm_create_args* a, gm_engine* e) {
   e->stream = e->own_stream;
   for (int s = 0; s < 5; ++s)
     for (int t = 0; t < 2; ++t) GM_CUDA(e, cudaEventCreate(&e->ev[s][t]));
-  GM_CUDA(e, cudaHostAlloc((void**)&e->h_status, sizeof(int) * 8, cudaHostAllocDefault));
+  GM_CUDA(e, cudaHostAlloc((void**)&e->h_status, sizeof(int) * (1 + (size_t)np * e->R), cudaHostAllocDefault));
 
   int rc;
   Csr csr;
-  if ((rc = make_csr(e, a, csr))) return rc;
+  std::vector<long long> prow0(np + 1, 0);
+  for (int p = 0; p < np; ++p) {
+    Csr one;
+    if ((rc = make_csr(e, probs[p], one))) return rc;
+    prow0[p + 1] = prow0[p] + probs[p].n;
+    if (np == 1) csr = std::move(one);
+    else append_block(csr, one, prow0[p]);
+  }
+  e->nnz = csr.ptr.back();
   // The mixed engine stores A / 2^e (e = floor(log2 of the largest absolute
   // row sum)) so that A's spectrum, the polynomial coefficients and the
   // Horner intermediates stay inside FP32's exponent range.  The scaling is a
@@ -454,9 +563,9 @@ int create_impl(const gm_create_args* a, gm_engine* e) {
     }
     e->scale_exp = mx > 0.0 ? (int)std::floor(std::log2(mx)) : 0;
   }
-  std::vector<long long> slot_rows, slice_off;
-  rc = e->prec == GM_FP64 ? upload_sell<double>(e, csr, a->sell_sigma, 0, slot_rows, slice_off)
-                          : upload_sell<float>(e, csr, a->sell_sigma, e->scale_exp, slot_rows, slice_off);
+  std::vector<long long> slot_rows, slice_off, pslice0;
+  rc = e->prec == GM_FP64 ? upload_sell<double>(e, csr, a->sell_sigma, 0, prow0, slot_rows, slice_off, pslice0)
+                          : upload_sell<float>(e, csr, a->sell_sigma, e->scale_exp, prow0, slot_rows, slice_off, pslice0);
   if (rc) return rc;
   // Column staging: per warp two stages of stage_cap * 32 column indices
   // (slices with more columns are read from global memory directly).
@@ -468,9 +577,9 @@ int create_impl(const gm_create_args* a, gm_engine* e) {
   // Grid: blocks_per_sm x SMs, capped by co-residency of each phase-group
   // kernel and by the work (about one SELL slice per warp: small problems
   // get fewer blocks, which makes every grid barrier cheaper).
-  const long long nsl = (e->n + 31) / 32;
+  const long long nsl = (long long)slice_off.size() - 1;
   const int nw = e->threads / 32;
-  const long long want = std::max<long long>(1, (nsl + nw - 1) / nw);
+  const long long want = std::max<long long>(np, (nsl + nw - 1) / nw);
   long long Gmax = 0;
   for (int g = 0; g < KGRP_N; ++g) {
     e->kfn[g] = pick_kernel(e->prec, e->R, g);
@@ -487,11 +596,9 @@ int create_impl(const gm_create_args* a, gm_engine* e) {
     e->Gk[g] = (int)std::max<long long>(1, G);
     Gmax = Gmax == 0 ? e->Gk[g] : std::min(Gmax, (long long)e->Gk[g]);
   }
-  // one grid size for every group: the slice partition is per block
-  for (int g = 0; g < KGRP_N; ++g) e->Gk[g] = (int)Gmax;
   e->G = (int)Gmax;
-
-  if ((rc = build_partition(e, csr, slot_rows, slice_off))) return rc;
+  // blocks per problem and the slice partition (sets e->G to the blocks used)
+  if ((rc = build_partition(e, csr, slot_rows, slice_off, pslice0, prow0))) return rc;
   e->kp.dep_mode = a->sync_policy == 0 ? 1 : 0;
   csr = Csr();
 
@@ -507,24 +614,30 @@ int create_impl(const gm_create_args* a, gm_engine* e) {
 
   double *gam, *gsr, *gsi, *wts, *shf, *flam = nullptr, *Q = nullptr, *mass, *ode;
   {
+    // per-problem method arrays, concatenated in problem order
     const int se = e->scale_exp;
-    std::vector<double> g(a->gamma, a->gamma + d + 1);
-    std::vector<double> gr(a->gamma_s_real, a->gamma_s_real + (size_t)(d + 1) * C);
-    std::vector<double> gi(a->gamma_s_imag, a->gamma_s_imag + (size_t)(d + 1) * C);
-    std::vector<double> w(a->wts, a->wts + (size_t)2 * C * R);
-    std::vector<double> sh(a->shifts, a->shifts + (size_t)2 * m * C * R);
-    if (se != 0) {
-      for (int i = 0; i <= d; ++i) {
-        g[i] = std::ldexp(g[i], se * (d - i));
-        for (int j = 0; j < C; ++j) {
-          gr[i + (size_t)(d + 1) * j] = std::ldexp(gr[i + (size_t)(d + 1) * j], se * (d - i));
-          gi[i + (size_t)(d + 1) * j] = std::ldexp(gi[i + (size_t)(d + 1) * j], se * (d - i));
+    std::vector<double> g, gr, gi, w, sh;
+    for (int p = 0; p < np; ++p) {
+      const ProbIn& q = probs[p];
+      const size_t g0 = g.size(), gr0 = gr.size(), w0 = w.size(), sh0 = sh.size();
+      g.insert(g.end(), q.gamma, q.gamma + d + 1);
+      gr.insert(gr.end(), q.gs_re, q.gs_re + (size_t)(d + 1) * C);
+      gi.insert(gi.end(), q.gs_im, q.gs_im + (size_t)(d + 1) * C);
+      w.insert(w.end(), q.wts, q.wts + (size_t)2 * C * R);
+      sh.insert(sh.end(), q.shifts, q.shifts + (size_t)2 * m * C * R);
+      if (se != 0) {
+        for (int i = 0; i <= d; ++i) {
+          g[g0 + i] = std::ldexp(g[g0 + i], se * (d - i));
+          for (int j = 0; j < C; ++j) {
+            gr[gr0 + i + (size_t)(d + 1) * j] = std::ldexp(gr[gr0 + i + (size_t)(d + 1) * j], se * (d - i));
+            gi[gr0 + i + (size_t)(d + 1) * j] = std::ldexp(gi[gr0 + i + (size_t)(d + 1) * j], se * (d - i));
+          }
         }
+        for (size_t t = w0; t < w.size(); ++t) w[t] = std::ldexp(w[t], -se);
+        for (size_t t = sh0; t < sh.size(); ++t) sh[t] = std::ldexp(sh[t], -se);
       }
-      for (auto& v : w) v = std::ldexp(v, -se);
-      for (auto& v : sh) v = std::ldexp(v, -se);
     }
-    if ((rc = dupload(e, &gam, g.data(), d + 1))) return rc;
+    if ((rc = dupload(e, &gam, g.data(), g.size()))) return rc;
     if ((rc = dupload(e, &gsr, gr.data(), gr.size()))) return rc;
     if ((rc = dupload(e, &gsi, gi.data(), gi.size()))) return rc;
     if ((rc = dupload(e, &wts, w.data(), w.size()))) return rc;
@@ -535,13 +648,13 @@ int create_impl(const gm_create_args* a, gm_engine* e) {
     if ((rc = dupload(e, &Q, a->Q, (size_t)k * n))) return rc;
   }
   std::vector<double> ones;
-  if (a->mass) {
+  if (a->mass && np == 1) {
     if ((rc = dupload(e, &mass, a->mass, n))) return rc;
   } else {
     ones.assign(n, 1.0);
     if ((rc = dupload(e, &mass, ones.data(), n))) return rc;
   }
-  if (a->ode) {
+  if (a->ode && np == 1) {
     if ((rc = dupload(e, &ode, a->ode, n))) return rc;
   } else {
     if ((rc = dalloc(e, &ode, n))) return rc;
@@ -559,6 +672,7 @@ int create_impl(const gm_create_args* a, gm_engine* e) {
 
   const size_t nR = (size_t)n * R;
   const size_t bsz = e->prec == GM_FP64 ? 8 : 4;
+  const size_t PR = (size_t)np * R;   // (problem, right-hand side) pairs
   if ((rc = dalloc(e, &kp.U, nR))) return rc;
   if ((rc = dalloc(e, &kp.Usol, nR))) return rc;
   if ((rc = dalloc(e, &kp.upd, nR))) return rc;
@@ -574,31 +688,41 @@ int create_impl(const gm_create_args* a, gm_engine* e) {
   if ((rc = dalloc(e, &H1, nR))) return rc;
   if ((rc = dalloc(e, &P, d > 0 ? (size_t)(d + 1) * nR : 1))) return rc;
   kp.V = V; kp.W0 = W0; kp.W1 = W1; kp.H0 = H0; kp.H1 = H1; kp.P = P;
-  if ((rc = dalloc(e, &kp.aabb, (size_t)(m + 1) * 2 * R))) return rc;
-  if ((rc = dalloc(e, &kp.Yr, (size_t)m * R * C))) return rc;
-  if ((rc = dalloc(e, &kp.Yi, (size_t)m * R * C))) return rc;
-  if ((rc = dalloc(e, &kp.coef, (size_t)R * (d + 1) * m))) return rc;
-  if ((rc = dalloc(e, &kp.coef_ff, (size_t)R * (d + 1) * m))) return rc;
-  if ((rc = dalloc(e, &kp.tri, (size_t)4 * m * R * C))) return rc;
+  if ((rc = dalloc(e, &kp.aabb, (size_t)(m + 1) * 2 * PR))) return rc;
+  if ((rc = dalloc(e, &kp.Yr, (size_t)m * PR * C))) return rc;
+  if ((rc = dalloc(e, &kp.Yi, (size_t)m * PR * C))) return rc;
+  if ((rc = dalloc(e, &kp.coef, PR * (d + 1) * m))) return rc;
+  if ((rc = dalloc(e, &kp.coef_ff, PR * (d + 1) * m))) return rc;
+  if ((rc = dalloc(e, &kp.tri, (size_t)4 * m * PR * C))) return rc;
   if ((rc = dalloc(e, &kp.Z, (size_t)(k + 4) * R))) return rc;
   if ((rc = dalloc(e, &kp.part, (size_t)(2 * R + (k + 4) * R) * e->G))) return rc;
-  if ((rc = dalloc(e, &kp.bar, 2))) return rc;
+  if ((rc = dalloc(e, &kp.bar, 2 + 2 * (size_t)np))) return rc;
   if ((rc = dalloc(e, &kp.status, 1))) return rc;
-  if ((rc = dalloc(e, &kp.meff, R))) return rc;
-  GM_CUDA(e, cudaMemset(kp.bar, 0, 2 * sizeof(unsigned)));
+  if ((rc = dalloc(e, &kp.meff, PR))) return rc;
+  GM_CUDA(e, cudaMemset(kp.bar, 0, (2 + 2 * (size_t)np) * sizeof(unsigned)));
   GM_CUDA(e, cudaMemset(kp.status, 0, sizeof(int)));
-  GM_CUDA(e, cudaMemset(kp.aabb, 0, (size_t)(m + 1) * 2 * R * sizeof(double)));
+  GM_CUDA(e, cudaMemset(kp.aabb, 0, (size_t)(m + 1) * 2 * PR * sizeof(double)));
   GM_CUDA(e, cudaMemset(kp.X, 0, nR * sizeof(double)));
-  GM_CUDA(e, cudaMemset(kp.Yr, 0, (size_t)m * R * C * sizeof(double)));
-  GM_CUDA(e, cudaMemset(kp.Yi, 0, (size_t)m * R * C * sizeof(double)));
+  GM_CUDA(e, cudaMemset(kp.Yr, 0, (size_t)m * PR * C * sizeof(double)));
+  GM_CUDA(e, cudaMemset(kp.Yi, 0, (size_t)m * PR * C * sizeof(double)));
   {
-    std::vector<int> me(R, m);
-    GM_CUDA(e, cudaMemcpy(kp.meff, me.data(), R * sizeof(int), cudaMemcpyHostToDevice));
+    std::vector<int> me(PR, m);
+    GM_CUDA(e, cudaMemcpy(kp.meff, me.data(), PR * sizeof(int), cudaMemcpyHostToDevice));
   }
   GM_CUDA(e, cudaDeviceSynchronize());
 
-  // constructor: scale columns, Usol = U, deflate (lanczos_impl.cu:79-89)
-  if ((rc = set_usol(e, a->U, false))) return rc;
+  // constructor: scale columns, Usol = U, deflate (lanczos_impl.cu:79-89);
+  // a batch's right-hand sides are stacked problem after problem per column
+  std::vector<double> Uall;
+  const double* U0 = probs[0].U;
+  if (np > 1) {
+    Uall.resize(nR);
+    for (int r = 0; r < R; ++r)
+      for (int p = 0; p < np; ++p)
+        std::memcpy(Uall.data() + (size_t)r * n + prow0[p], probs[p].U + (size_t)r * probs[p].n, sizeof(double) * probs[p].n);
+    U0 = Uall.data();
+  }
+  if ((rc = set_usol(e, U0, false))) return rc;
   const int saved = e->sync_mode;
   e->sync_mode = 1;
   rc = launch(e, gm::PH_DEFLATE, 0);
@@ -634,7 +758,38 @@ int gm_lanczos_create(const gm_create_args* args, gm_handle* out) {
   *out = nullptr;
   gm_engine* e = new (std::nothrow) gm_engine();
   if (!e) return fail(nullptr, GM_ERR_OOM, "host allocation failed");
-  int rc = create_impl(args, e);
+  if (!args->ptr || !args->ind || !args->values || args->n <= 0) {
+    // report shape errors under the reference's identifiers before any device work
+    delete e;
+    if (args->n <= 0) return fail(nullptr, GM_ERR_ARG, "lanczos_create:inputNotSquare: n must be positive");
+    return fail(nullptr, GM_ERR_ARG, "lanczos_create:inputNotSparse: null sparse array");
+  }
+  ProbIn q{args->n, args->nnz, args->format, reinterpret_cast<const long long*>(args->ptr),
+           reinterpret_cast<const long long*>(args->ind), args->values, args->U, args->gamma,
+           args->gamma_s_real, args->gamma_s_imag, args->wts, args->shifts};
+  int rc = create_impl(args, std::vector<ProbIn>{q}, e);
+  if (rc) {
+    g_create_error = e->err;
+    destroy(e);
+    return rc;
+  }
+  *out = e;
+  return GM_OK;
+}
+
+int gm_batch_create(int nprob, const gm_batch_problem* probs, const gm_create_args* common, gm_handle* out) {
+  g_create_error.clear();
+  if (!probs || !common || !out || nprob < 1) return fail(nullptr, GM_ERR_ARG, "batch_create: null argument or no problems");
+  *out = nullptr;
+  gm_engine* e = new (std::nothrow) gm_engine();
+  if (!e) return fail(nullptr, GM_ERR_OOM, "host allocation failed");
+  std::vector<ProbIn> v;
+  for (int p = 0; p < nprob; ++p) {
+    const gm_batch_problem& b = probs[p];
+    v.push_back(ProbIn{b.n, 0, b.format, reinterpret_cast<const long long*>(b.ptr), reinterpret_cast<const long long*>(b.ind),
+                       b.values, b.U, b.gamma, b.gamma_s_real, b.gamma_s_imag, b.wts, b.shifts});
+  }
+  int rc = create_impl(common, v, e);
   if (rc) {
     g_create_error = e->err;
     destroy(e);
@@ -709,21 +864,25 @@ int gm_get_solution(gm_handle h, double* dst) {
 
 int gm_get_aabb(gm_handle h, double* dst) {
   if (!h || !dst) return GM_ERR_ARG;
-  GM_CUDA(h, cudaMemcpyAsync(dst, h->kp.aabb, (size_t)(h->m + 1) * 2 * h->R * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  GM_CUDA(h, cudaMemcpyAsync(dst, h->kp.aabb, (size_t)(h->m + 1) * 2 * h->R * h->nprob * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   int rc = check_sync(h);
   if (h->scale_exp != 0) {
     // alpha_j and beta_{j>=1} of the scaled operator are those of A over 2^e
     const size_t ld = h->m + 1;
-    for (int r = 0; r < 2 * h->R; ++r)
-      for (size_t q = 0; q < ld; ++q)
-        if (r < h->R || q > 0) dst[r * ld + q] = std::ldexp(dst[r * ld + q], h->scale_exp);
+    for (int p = 0; p < h->nprob; ++p)
+      for (int r = 0; r < 2 * h->R; ++r)
+        for (size_t q = 0; q < ld; ++q)
+          if (r < h->R || q > 0) {
+            double& v = dst[((size_t)p * 2 * h->R + r) * ld + q];
+            v = std::ldexp(v, h->scale_exp);
+          }
   }
   return rc;
 }
 
 int gm_get_y(gm_handle h, double* yr, double* yi) {
   if (!h) return GM_ERR_ARG;
-  const size_t cnt = (size_t)h->m * h->R * h->C;
+  const size_t cnt = (size_t)h->m * h->R * h->C * h->nprob;
   if (yr) GM_CUDA(h, cudaMemcpyAsync(yr, h->kp.Yr, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   if (yi) GM_CUDA(h, cudaMemcpyAsync(yi, h->kp.Yi, cnt * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   return check_sync(h);
@@ -731,7 +890,7 @@ int gm_get_y(gm_handle h, double* yr, double* yi) {
 
 int gm_set_y(gm_handle h, const double* yr, const double* yi) {
   if (!h || !yr || !yi) return fail(h, GM_ERR_ARG, "set_y: null argument");
-  const size_t cnt = (size_t)h->m * h->R * h->C;
+  const size_t cnt = (size_t)h->m * h->R * h->C * h->nprob;
   GM_CUDA(h, cudaMemcpyAsync(h->kp.Yr, yr, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   GM_CUDA(h, cudaMemcpyAsync(h->kp.Yi, yi, cnt * sizeof(double), cudaMemcpyHostToDevice, h->stream));
   int rc = launch(h, gm::PH_COEF, 2);
@@ -742,7 +901,7 @@ int gm_set_y(gm_handle h, const double* yr, const double* yi) {
 int gm_get_meff(gm_handle h, int* meff) {
   if (!h || !meff) return GM_ERR_ARG;
   int rc = check_sync(h);
-  for (int r = 0; r < h->R; ++r) meff[r] = h->h_status[1 + r];
+  for (int r = 0; r < h->R * h->nprob; ++r) meff[r] = h->h_status[1 + r];
   return rc;
 }
 
@@ -776,6 +935,59 @@ int gm_solve_host(gm_handle h, const double* b_host, double* x_host) {
   return gm_get_solution(h, x_host);
 }
 
+int gm_time_loop(gm_handle h, int nsteps, int mode, int use_graph) {
+  if (!h) return GM_ERR_ARG;
+  if (nsteps < 0 || (mode != 0 && mode != 1)) return fail(h, GM_ERR_ARG, "time_loop: nsteps >= 0 and mode 0 or 1");
+  if (h->R != 2) return fail(h, GM_ERR_ARG, "time_loop needs nrhs = 2 (solution and reaction columns)");
+  const int solve = gm::PH_LANCZOS | gm::PH_TRISOLVE | gm::PH_COEF | gm::PH_APPLY | gm::PH_APPLY_SET;
+  const int upd = (mode == 0 ? gm::PH_UPDATE_FKPP : gm::PH_UPDATE_FHN) | gm::PH_DEFLATE;
+  const int saved = h->sync_mode;
+  h->sync_mode = 0;
+  int rc = GM_OK;
+  if (!use_graph) {
+    for (int t = 0; t < nsteps && rc == GM_OK; ++t) {
+      rc = launch(h, solve, 4);
+      if (rc == GM_OK) rc = launch(h, upd, 0);
+    }
+  } else {
+    if (!h->loop_exec || h->loop_steps != nsteps || h->loop_mode != mode) {
+      if (h->loop_exec) {
+        cudaGraphExecDestroy(h->loop_exec);
+        h->loop_exec = nullptr;
+      }
+      cudaGraph_t graph = nullptr;
+      GM_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+      h->capturing = true;
+      for (int t = 0; t < nsteps && rc == GM_OK; ++t) {
+        rc = launch(h, solve, 4);
+        if (rc == GM_OK) rc = launch(h, upd, 0);
+      }
+      h->capturing = false;
+      cudaError_t st = cudaStreamEndCapture(h->stream, &graph);
+      if (rc == GM_OK && st != cudaSuccess) rc = cuda_fail(h, st, "cudaStreamEndCapture");
+      if (rc == GM_OK) {
+        st = cudaGraphInstantiate(&h->loop_exec, graph, 0);
+        if (st != cudaSuccess) rc = cuda_fail(h, st, "cudaGraphInstantiate");
+      }
+      if (graph) cudaGraphDestroy(graph);
+      if (rc != GM_OK) {
+        h->sync_mode = saved;
+        return rc;
+      }
+      h->loop_steps = nsteps;
+      h->loop_mode = mode;
+    }
+    GM_CUDA(h, cudaEventRecord(h->ev[4][0], h->stream));
+    GM_CUDA(h, cudaGraphLaunch(h->loop_exec, h->stream));
+    GM_CUDA(h, cudaEventRecord(h->ev[4][1], h->stream));
+    h->ev_used[4] = true;
+  }
+  h->sync_mode = saved;
+  h->have_V = h->have_y = h->have_coef = true;
+  if (rc == GM_OK && saved) rc = check_sync(h);
+  return rc;
+}
+
 int gm_sync(gm_handle h) {
   if (!h) return GM_ERR_ARG;
   return check_sync(h);
@@ -803,6 +1015,7 @@ int gm_info(gm_handle h, int64_t* info) {
   info[0] = h->n; info[1] = h->R; info[2] = h->m; info[3] = h->d; info[4] = h->C; info[5] = h->k;
   info[6] = h->prec; info[7] = h->G; info[8] = h->threads; info[9] = h->padded;
   info[10] = (int64_t)h->bytes; info[11] = h->launches;
+  info[12] = h->nprob;
   return GM_OK;
 }
 

@@ -76,6 +76,10 @@ struct KParams {
   unsigned long long* prog;   // [G] pass progress flags
   unsigned long long epoch;   // launch counter
   int dep_mode;               // 1: neighbour waits between SpMV passes, 0: grid barriers
+  int nprob;                  // independent problems in this launch (0 or 1: one problem)
+  const int* blk_prob;        // [G] problem of each block
+  const int* prob_blk0;       // [nprob+1] first block of each problem
+  const long long* prob_row0; // [nprob+1] first row of each problem
   int stage_cap;              // >0: stage each slice's column indices in shared memory by TMA
                               // bulk copies (slices of at most stage_cap columns); 0: off
   int* status;
@@ -115,6 +119,33 @@ struct PassSync {
   }
   __device__ bool before_next() {
     return mode ? dep.wait(pc) : bar.sync();
+  }
+};
+
+// The block's problem group.  A launch can carry several independent
+// problems (a batch); each owns a contiguous range of blocks, rows and SELL
+// slices, its own barrier and its own reductions.  One problem is the
+// single-group case.
+struct Grp {
+  int p, gb, Gp, bl;
+  long long r0, r1, gt, tt;
+  __device__ Grp(const KParams& kp, const Ctx& c) {
+    if (kp.nprob > 0) {
+      p = kp.blk_prob[c.b];
+      gb = kp.prob_blk0[p];
+      Gp = kp.prob_blk0[p + 1] - gb;
+      r0 = kp.prob_row0[p];
+      r1 = kp.prob_row0[p + 1];
+    } else {
+      p = 0; gb = 0; Gp = c.G; r0 = 0; r1 = kp.n;
+    }
+    bl = c.b - gb;
+    gt = r0 + (long long)bl * c.nt + c.tid;
+    tt = (long long)Gp * c.nt;
+  }
+  // barrier over this group's blocks (words 2 + 2p, 3 + 2p of kp.bar)
+  __device__ GridBar bar(const KParams& kp) const {
+    return GridBar{kp.bar + 2 + 2 * p, kp.bar + 3 + 2 * p, kp.status, (unsigned)Gp, kp.timeout_ns};
   }
 };
 
@@ -315,13 +346,13 @@ struct LanczosScalars {
 // Every block sums the G per-block partials (layout [R][G]) in one fixed
 // order into dst (shared memory); deterministic and identical in all blocks.
 template <int N>
-__device__ __forceinline__ void grid_total_smem(const double* partials, int G, double* dst) {
+__device__ __forceinline__ void grid_total_smem(const double* partials, int stride, int count, double* dst) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (warp == 0) {
 #pragma unroll
     for (int j = 0; j < N; ++j) {
       double t = 0.0;
-      for (int b = lane; b < G; b += 32) t += partials[(long long)j * G + b];
+      for (int b = lane; b < count; b += 32) t += partials[(long long)j * stride + b];
       t = warp_sum(t);
       if (lane == 0) dst[j] = t;
     }
@@ -330,13 +361,16 @@ __device__ __forceinline__ void grid_total_smem(const double* partials, int G, d
 }
 
 template <class Pol, int R>
-__device__ bool phase_lanczos(const KParams& kp, const Ctx& c, PassSync& ps, ColStage& cs) {
+__device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, PassSync& ps, ColStage& cs) {
   using BT = typename Pol::BT;
   using HT = typename Pol::HT;
   using AT = typename Pol::AT;
   const long long n = kp.n;
   const int m = kp.m, d = kp.d, G = kp.G;
-  GridBar bar{kp.bar, kp.bar + 1, kp.status, (unsigned)G, kp.timeout_ns};
+  GridBar bar = g.bar(kp);
+  double* const aab = kp.aabb + (long long)(m + 1) * 2 * R * g.p;   // this problem's aabb
+  int* const meff = kp.meff + (long long)R * g.p;
+  const double* const gam = kp.gamma + (long long)(d + 1) * g.p;
   BT* V = reinterpret_cast<BT*>(kp.V);
   BT* const W0 = reinterpret_cast<BT*>(kp.W0);
   BT* const W1 = reinterpret_cast<BT*>(kp.W1);
@@ -351,7 +385,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, PassSync& ps, Col
     double bp[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) bp[r] = 0.0;
-    for (long long i = c.gt; i < n; i += c.tt) {
+    for (long long i = g.gt; i < g.r1; i += g.tt) {
       double u[R];
       VecIO<R>::ld(kp.U + i * R, u);
       BT wb[R];
@@ -362,15 +396,15 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, PassSync& ps, Col
     block_sum_store<R>(bp, part_b + c.b, G);
   }
   if (!bar.sync()) return false;
-  grid_total_smem<R>(part_b, G, sh.tot);
+  grid_total_smem<R>(part_b + g.gb, G, g.Gp, sh.tot);
   if (c.tid == 0) {
     for (int r = 0; r < R; ++r) {
       sh.beta[r] = sqrt(sh.tot[r]);
       sh.broken[r] = !(sh.beta[r] > 0.0);
       sh.rbeta[r] = sh.broken[r] ? 0.0 : 1.0 / sh.beta[r];
-      if (c.b == 0) {
-        kp.aabb[(long long)(m + 1) * (R + r)] = sh.beta[r];
-        kp.meff[r] = sh.broken[r] ? 0 : m;
+      if (g.bl == 0) {
+        aab[(long long)(m + 1) * (R + r)] = sh.beta[r];
+        meff[r] = sh.broken[r] ? 0 : m;
         if (!(sh.tot[r] == sh.tot[r]) || isinf(sh.tot[r])) atomicCAS(kp.status, 0, (int)ST_NONFINITE);
       }
     }
@@ -383,7 +417,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, PassSync& ps, Col
     BT* Wout = (j & 1) ? W1 : W0;
     if (c.tid == 0) {
       for (int r = 0; r < R; ++r) {
-        sh.sc[r] = Pol::scalar(sh.rbeta[r] * kp.gamma[0]);
+        sh.sc[r] = Pol::scalar(sh.rbeta[r] * gam[0]);
         sh.rb[r] = Pol::scalar(sh.rbeta[r]);
         sh.bj[r] = Pol::scalar(sh.beta[r]);
       }
@@ -418,7 +452,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, PassSync& ps, Col
     } else {
       // Horner pass 1: u = gamma_1 v_j + A (gamma_0 v_j); stores v_j
       {
-        const typename Pol::ST g1 = Pol::scalar(kp.gamma[1]);
+        const typename Pol::ST g1 = Pol::scalar(gam[1]);
         spmv_pass<Pol, R, BT>(kp, c, cs, src, [&](long long s, AT (&z)[R]) {
           const long long row = slot_row(kp, s, c.lane);
           if (row < 0) return;
@@ -436,7 +470,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, PassSync& ps, Col
       ps.done();
       if (!ps.before_next()) return false;
       for (int h = 2; h <= d; ++h) {
-        const typename Pol::ST gh = Pol::scalar(kp.gamma[h]);
+        const typename Pol::ST gh = Pol::scalar(gam[h]);
         const HT* hin = (h & 1) ? H0 : H1;
         HT* hout = (h & 1) ? H1 : H0;
         spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
@@ -482,7 +516,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, PassSync& ps, Col
     }
     ps.done();
     if (!bar.sync()) return false;
-    grid_total_smem<R>(part_a, G, sh.alpha);
+    grid_total_smem<R>(part_a + g.gb, G, g.Gp, sh.alpha);
     if (c.tid == 0) {
       for (int r = 0; r < R; ++r) sh.al[r] = Pol::scalar(sh.alpha[r]);
     }
@@ -492,7 +526,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, PassSync& ps, Col
       AT bpa[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) bpa[r] = Pol::zero();
-      for (long long i = c.gt; i < n; i += c.tt) {
+      for (long long i = g.gt; i < g.r1; i += g.tt) {
         BT wb[R], v[R];
         VecIO<R>::ld(Wout + i * R, wb);
         VecIO<R>::ld(Vj + i * R, v);
@@ -510,21 +544,21 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, PassSync& ps, Col
       block_sum_store<R>(bp, part_b + c.b, G);
     }
     if (!bar.sync()) return false;
-    grid_total_smem<R>(part_b, G, sh.tot);
+    grid_total_smem<R>(part_b + g.gb, G, g.Gp, sh.tot);
     if (c.tid == 0) {
       int all = 1;
       for (int r = 0; r < R; ++r) {
         const double bn = sqrt(sh.tot[r]);
         const double al = sh.alpha[r];
-        if (c.b == 0) {
-          kp.aabb[j + (long long)(m + 1) * r] = sh.broken[r] ? 0.0 : al;
-          kp.aabb[(j + 1) + (long long)(m + 1) * (R + r)] = sh.broken[r] ? 0.0 : bn;
+        if (g.bl == 0) {
+          aab[j + (long long)(m + 1) * r] = sh.broken[r] ? 0.0 : al;
+          aab[(j + 1) + (long long)(m + 1) * (R + r)] = sh.broken[r] ? 0.0 : bn;
           if (!(bn == bn) || isinf(bn) || !(al == al)) atomicCAS(kp.status, 0, (int)ST_NONFINITE);
         }
         const double scale = fabs(al) + (j > 0 ? sh.beta[r] : 0.0);
         if (!sh.broken[r] && j + 1 < m && !(bn > kp.bd_tol * scale)) {
           sh.broken[r] = 1;
-          if (c.b == 0) kp.meff[r] = j + 1;
+          if (g.bl == 0) meff[r] = j + 1;
         }
         sh.beta[r] = sh.broken[r] ? 0.0 : bn;
         sh.rbeta[r] = sh.broken[r] ? 0.0 : 1.0 / bn;
@@ -552,18 +586,23 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, PassSync& ps, Col
 template <int R>
 __device__ void phase_trisolve(const KParams& kp, const Ctx& c) {
   const int m = kp.m, C = kp.C;
+  const int np = kp.nprob > 0 ? kp.nprob : 1;
   if (c.lane != 0) return;
-  for (long long sys = c.gw; sys < (long long)R * C; sys += c.tw) {
-    const int r = (int)(sys / C), j = (int)(sys % C);
-    const int me = kp.meff[r];
-    const double* __restrict__ al = kp.aabb + (long long)(m + 1) * r;
-    const double* __restrict__ be = kp.aabb + (long long)(m + 1) * (R + r);
+  for (long long sys = c.gw; sys < (long long)np * R * C; sys += c.tw) {
+    // sys = (p R + r) C + j for problem p, right-hand side r, node j
+    const long long rr = sys / C;
+    const int j = (int)(sys % C);
+    const long long p = rr / R;
+    const int r = (int)(rr % R);
+    const int me = kp.meff[rr];
+    const double* __restrict__ al = kp.aabb + (long long)(m + 1) * (2 * R * p + r);
+    const double* __restrict__ be = kp.aabb + (long long)(m + 1) * (2 * R * p + R + r);
     const double* __restrict__ sh = kp.shifts + 2LL * m * sys;
     double* __restrict__ ig = kp.tri + 4LL * m * sys;  // 1/g_q (re, im)
     double* __restrict__ yr = kp.Yr + (long long)m * sys;
     double* __restrict__ yi = kp.Yi + (long long)m * sys;
     const double b0 = be[0];
-    const double wr = kp.wts[2LL * C * r + j], wi = kp.wts[2LL * C * r + C + j];
+    const double wr = kp.wts[2LL * C * rr + j], wi = kp.wts[2LL * C * rr + C + j];
     double igr = 0.0, igi = 0.0;   // 1/g_{q+1}
     for (int q = me - 1; q >= 0; --q) {
       const double b2 = q + 1 < me ? be[q + 1] * be[q + 1] : 0.0;
@@ -601,16 +640,21 @@ __device__ void phase_trisolve(const KParams& kp, const Ctx& c) {
 template <int R>
 __device__ void phase_coef(const KParams& kp, const Ctx& c) {
   const int m = kp.m, C = kp.C, d1 = kp.d + 1;
-  const long long total = (long long)R * d1 * m;
+  const int np = kp.nprob > 0 ? kp.nprob : 1;
+  const long long total = (long long)np * R * d1 * m;
   for (long long t = c.gt; t < total; t += c.tt) {
+    // t = (rr d1 + i) m + q with rr = p R + r
     const int q = (int)(t % m);
     const int i = (int)((t / m) % d1);
-    const int r = (int)(t / ((long long)m * d1));
+    const long long rr = t / ((long long)m * d1);
+    const long long p = rr / R;
+    const double* gr = kp.gs_re + (long long)d1 * C * p;
+    const double* gi = kp.gs_im + (long long)d1 * C * p;
     double acc = 0.0;
     for (int j = 0; j < C; ++j) {
-      const long long col = (long long)r * C + j;
-      acc = fma(kp.gs_re[i + (long long)d1 * j], kp.Yi[col * m + q], acc);
-      acc = fma(kp.gs_im[i + (long long)d1 * j], kp.Yr[col * m + q], acc);
+      const long long col = rr * C + j;
+      acc = fma(gr[i + (long long)d1 * j], kp.Yi[col * m + q], acc);
+      acc = fma(gi[i + (long long)d1 * j], kp.Yr[col * m + q], acc);
     }
     kp.coef[t] = acc;
     const float h = (float)acc;
@@ -622,13 +666,13 @@ __device__ void phase_coef(const KParams& kp, const Ctx& c) {
 // X_r += sum_i A^(d-i) V_r c_{r,i}: one lift pass P_i = V c_i (V read once),
 // then d Horner passes X = A X + P_i.
 template <class Pol, int R>
-__device__ bool phase_apply(const KParams& kp, const Ctx& c, bool overwrite, PassSync& ps, ColStage& cs) {
+__device__ bool phase_apply(const KParams& kp, const Ctx& c, const Grp& g, bool overwrite, PassSync& ps,
+                            ColStage& cs) {
   using BT = typename Pol::BT;
   using HT = typename Pol::HT;
   using AT = typename Pol::AT;
   const long long n = kp.n;
   const int m = kp.m, d = kp.d, d1 = d + 1;
-  GridBar bar{kp.bar, kp.bar + 1, kp.status, (unsigned)kp.G, kp.timeout_ns};
   const BT* V = reinterpret_cast<const BT*>(kp.V);
   HT* P = reinterpret_cast<HT*>(kp.P);
   HT* const H0 = reinterpret_cast<HT*>(kp.H0);
@@ -652,7 +696,7 @@ __device__ bool phase_apply(const KParams& kp, const Ctx& c, bool overwrite, Pas
           if (i0 + ii < d1) {
 #pragma unroll
             for (int r = 0; r < R; ++r) {
-              const long long ci = ((long long)r * d1 + i0 + ii) * m + q;
+              const long long ci = (((long long)R * g.p + r) * d1 + i0 + ii) * m + q;
               if constexpr (Pol::kMixed) {
                 const float2 cf = kp.coef_ff[ci];
                 acc[ii][r] = Pol::add(acc[ii][r], ff_mulf(ff{cf.x, cf.y}, v[r]));
@@ -859,7 +903,8 @@ __global__ void __launch_bounds__(512, (R >= 4 ? 1 : GM_MINB)) fab_kernel(KParam
   GridBar bar{kp.bar, kp.bar + 1, kp.status, (unsigned)kp.G, kp.timeout_ns};
   if (*(volatile int*)kp.status != 0) return;
   const int ph = kp.phases & PH;
-  PassSync ps{bar, make_dep(kp), kp.dep_mode, 0u};
+  const Grp g(kp, c);
+  PassSync ps{g.bar(kp), make_dep(kp), kp.dep_mode, 0u};
   ColStage cs;
   if (PH & (PH_LANCZOS | PH_APPLY)) cs.init(kp, c);
   bool first = true;
@@ -869,7 +914,7 @@ __global__ void __launch_bounds__(512, (R >= 4 ? 1 : GM_MINB)) fab_kernel(KParam
   };
   if ((PH & PH_LANCZOS) && (ph & PH_LANCZOS)) {
     if (!sep()) return;
-    if (!phase_lanczos<Pol, R>(kp, c, ps, cs)) return;
+    if (!phase_lanczos<Pol, R>(kp, c, g, ps, cs)) return;
   }
   if ((PH & PH_TRISOLVE) && (ph & PH_TRISOLVE)) {
     if (!sep()) return;
@@ -881,7 +926,7 @@ __global__ void __launch_bounds__(512, (R >= 4 ? 1 : GM_MINB)) fab_kernel(KParam
   }
   if ((PH & PH_APPLY) && (ph & PH_APPLY)) {
     if (!sep()) return;
-    if (!phase_apply<Pol, R>(kp, c, (ph & PH_APPLY_SET) != 0, ps, cs)) return;
+    if (!phase_apply<Pol, R>(kp, c, g, (ph & PH_APPLY_SET) != 0, ps, cs)) return;
   }
   if (PH & (PH_DEFLATE | PH_UPDATE_FKPP | PH_UPDATE_FHN)) {
     const int upd_mode = (ph & PH_UPDATE_FKPP) ? 1 : ((ph & PH_UPDATE_FHN) ? 2 : 0);

@@ -33,7 +33,7 @@ EXPORTED_SYMBOLS = [
     "gm_get_xsol", "gm_get_aabb", "gm_set_y", "gm_get_y", "gm_set_U", "gm_set_U_device", "gm_get_update",
     "gm_get_solution", "gm_solve", "gm_solve_host", "gm_sync", "gm_set_stream",
     "gm_phase_times", "gm_info", "gm_get_meff", "gm_last_error", "gm_version",
-    "gm_lin_sys_solves_noalloc",
+    "gm_lin_sys_solves_noalloc", "gm_batch_create", "gm_time_loop",
 ]
 
 _dp = ct.POINTER(ct.c_double)
@@ -62,6 +62,15 @@ class CreateArgs(ct.Structure):
     ]
 
 
+class BatchProblem(ct.Structure):
+    """ctypes mirror of gm_batch_problem."""
+    _fields_ = [
+        ("n", ct.c_int64), ("format", ct.c_int), ("ptr", _lp), ("ind", _lp), ("values", _dp),
+        ("U", _dp), ("gamma", _dp), ("gamma_s_real", _dp), ("gamma_s_imag", _dp),
+        ("wts", _dp), ("shifts", _dp),
+    ]
+
+
 _LIB = None
 
 
@@ -81,6 +90,7 @@ def load_library(build_if_missing: bool = False) -> ct.CDLL:
     lib.gm_default_args.argtypes = [ct.POINTER(CreateArgs)]
     lib.gm_default_args.restype = None
     lib.gm_lanczos_create.argtypes = [ct.POINTER(CreateArgs), ct.POINTER(h)]
+    lib.gm_batch_create.argtypes = [ct.c_int, ct.POINTER(BatchProblem), ct.POINTER(CreateArgs), ct.POINTER(h)]
     for name in ("gm_lanczos_delete", "gm_build_subspace", "gm_lin_sys_solves", "gm_apply_V",
                  "gm_update_U", "gm_update_U_monodomain", "gm_solve", "gm_sync"):
         getattr(lib, name).argtypes = [h]
@@ -92,6 +102,7 @@ def load_library(build_if_missing: bool = False) -> ct.CDLL:
     lib.gm_get_y.argtypes = [h, _dp, _dp]
     lib.gm_solve_host.argtypes = [h, _dp, _dp]
     lib.gm_set_stream.argtypes = [h, ct.c_void_p]
+    lib.gm_time_loop.argtypes = [h, ct.c_int, ct.c_int, ct.c_int]
     lib.gm_phase_times.argtypes = [h, ct.POINTER(ct.c_float)]
     lib.gm_info.argtypes = [h, _lp]
     lib.gm_get_meff.argtypes = [h, ct.POINTER(ct.c_int)]
@@ -271,6 +282,11 @@ class Engine:
         self._check(self._lib.gm_solve_host(self._h, bc.ctypes.data_as(_dp), out.ctypes.data_as(_dp)))
         return out
 
+    def time_loop(self, nsteps: int, monodomain: bool = False, graph: bool = True):
+        """nsteps exponential-Euler steps (fused solve + update_U or
+        update_U_monodomain), replayed from a cached CUDA graph by default."""
+        self._check(self._lib.gm_time_loop(self._h, int(nsteps), 1 if monodomain else 0, 1 if graph else 0))
+
     def sync(self):
         self._check(self._lib.gm_sync(self._h))
 
@@ -282,15 +298,17 @@ class Engine:
         self._check(self._lib.gm_phase_times(self._h, ms))
         return dict(zip(("deflate", "build_subspace", "lin_sys_solves", "apply_V", "solve"), list(ms)))
 
+    nprob = 1
+
     def info(self) -> dict:
-        v = (ct.c_int64 * 12)()
+        v = (ct.c_int64 * 13)()
         self._check(self._lib.gm_info(self._h, v))
         keys = ("n", "nrhs", "m", "d", "C", "k", "precision", "grid_blocks", "threads",
-                "sell_padded", "device_bytes", "launches")
+                "sell_padded", "device_bytes", "launches", "problems")
         return dict(zip(keys, list(v)))
 
     def meff(self) -> list:
-        v = (ct.c_int * self.R)()
+        v = (ct.c_int * (self.R * self.nprob))()
         self._check(self._lib.gm_get_meff(self._h, v))
         return list(v)
 
@@ -339,3 +357,71 @@ class LanczosEngine(Engine):
         kw.setdefault("matrix_format", "csc")
         super().__init__(A, U, Q, lambda_, flam, int(N), gamma, gamma_s_real, gamma_s_imag,
                          [wts1, wts2], shifts, dt=dt, col_scale=None, mass=mass, ode=ode, fhn=fhn, **kw)
+
+
+class BatchEngine(Engine):
+    """Several independent problems (uneven sizes) in one engine: every launch
+    runs all of them at once (gm_batch_create).  All problems share m, C, the
+    polynomial degree and the number of right-hand sides; vectors are the
+    problems' rows stacked in order."""
+
+    def __init__(self, problems: Sequence, precision: str | int = "fp64", sync: bool = True,
+                 threads: int = 0, blocks_per_sm: int = 0, sell_sigma: int = 0, timeout_s: float = 0.0,
+                 sync_policy: int = 0, col_staging: int = 0):
+        self._lib = load_library()
+        self._h = ct.c_void_p()
+        P0 = problems[0]
+        R, m, C, d1 = P0.R, P0.m, P0.C, P0.gamma.size
+        keep = []
+        arr = (BatchProblem * len(problems))()
+        for i, P in enumerate(problems):
+            if P.R != R or P.m != m or P.C != C or P.gamma.size != d1 or P.k != 0:
+                raise GmError(1, "batch_create: problems must share nrhs, m, C and degree, without deflation")
+            M = sp.csr_matrix(P.A)
+            ptr = np.ascontiguousarray(M.indptr, dtype=np.int64)
+            ind = np.ascontiguousarray(M.indices, dtype=np.int64)
+            val = _f64(M.data)
+            U = _f64(np.asarray(P.U).reshape(P.n, -1).T).reshape(-1)
+            gam = _f64(P.gamma)
+            gsr = _f64(np.asarray(P.gs_re).T).reshape(-1)
+            gsi = _f64(np.asarray(P.gs_im).T).reshape(-1)
+            wts = _f64(np.concatenate([_f64(w).reshape(C, 2).T.reshape(-1) for w in P.wts]))
+            sh = _f64(P.shifts)
+            keep.extend([ptr, ind, val, U, gam, gsr, gsi, wts, sh])
+            arr[i] = BatchProblem(P.n, GM_CSR, _ptr(ptr, _lp), _ptr(ind, _lp), _ptr(val), _ptr(U), _ptr(gam),
+                                  _ptr(gsr), _ptr(gsi), _ptr(wts), _ptr(sh))
+        a = CreateArgs()
+        self._lib.gm_default_args(ct.byref(a))
+        cs = np.ones(R)
+        keep.append(cs)
+        a.nrhs, a.subspace_size, a.gamma_size, a.contour_size = R, m, d1, C
+        a.col_scale = _ptr(cs)
+        a.precision = int({"fp64": GM_FP64, "mixed": GM_MIXED}.get(precision, precision))
+        a.sync_mode = 1 if sync else 0
+        a.threads_per_block, a.blocks_per_sm, a.sell_sigma = threads, blocks_per_sm, sell_sigma
+        a.barrier_timeout_s, a.sync_policy, a.col_staging = timeout_s, int(sync_policy), int(col_staging)
+        rc = self._lib.gm_batch_create(len(problems), arr, ct.byref(a), ct.byref(self._h))
+        del keep
+        if rc != 0:
+            raise GmError(rc, self._lib.gm_last_error(None).decode())
+        self.nprob = len(problems)
+        self.sizes = [P.n for P in problems]
+        self.row0 = np.concatenate([[0], np.cumsum(self.sizes)])
+        self.n, self.R, self.m, self.C, self.k, self.d = int(self.row0[-1]), R, m, C, 0, d1 - 1
+        self.precision = a.precision
+
+    def split(self, X: np.ndarray) -> list:
+        """Per-problem row blocks of a stacked (n_total, R) array."""
+        return [X[self.row0[p]:self.row0[p + 1]] for p in range(self.nprob)]
+
+    def get_aabb(self) -> np.ndarray:
+        """(nprob, m+1, 2R): alpha columns then beta columns per problem."""
+        out = np.empty((self.m + 1) * 2 * self.R * self.nprob)
+        self._check(self._lib.gm_get_aabb(self._h, _ptr(out)))
+        return out.reshape(self.nprob, 2 * self.R, self.m + 1).transpose(0, 2, 1).copy()
+
+    def get_y(self):
+        cnt = self.m * self.R * self.C * self.nprob
+        yr, yi = np.empty(cnt), np.empty(cnt)
+        self._check(self._lib.gm_get_y(self._h, _ptr(yr), _ptr(yi)))
+        return yr.reshape(-1, self.m).T.copy(), yi.reshape(-1, self.m).T.copy()

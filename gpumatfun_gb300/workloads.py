@@ -241,3 +241,73 @@ def cached_problem(name: str, R: int = 1, cache_dir: str | None = None, seed: in
     os.replace(tmp, path)
     return make_problem(P.name, P.A, P.U[:, :R], P.Q, P.lam, [f] * R, 80, 48, P.l1, P.lN, degree=8,
                         prob_dim=P.lN / 4, meta=P.meta)
+
+
+def batch_sizes(nprob: int, lo: int = 64, hi: int = 1024, seed: int = 0) -> np.ndarray:
+    """Grid sides drawn log-uniformly in [lo, hi] from the seed."""
+    rng = np.random.default_rng(seed)
+    return np.round(np.exp(rng.uniform(math.log(lo), math.log(hi), nprob))).astype(int)
+
+
+def config5_batch(nprob: int = 64, R: int = 4, seed: int = 0, lo: int = 64, hi: int = 1024,
+                  m: int = 60, C: int = 32, alpha: float = 1.5, degree: int = 0) -> list:
+    """Batched serving-style workload: ``nprob`` independent fractional
+    diffusion problems f(A) b with f = x^(-alpha/2) on 2D 5-point Dirichlet
+    Laplacians (side N drawn log-uniformly in [lo, hi], scaled by (N+1)^2),
+    each with R right-hand sides, all solved by one launch."""
+    f = params.frac_power(-alpha / 2)
+    out = []
+    for i, N in enumerate(batch_sizes(nprob, lo, hi, seed)):
+        P = fd2d_problem(int(N), 0, m, C, [f] * R, R=R, scale=(N + 1.0) ** 2, seed=seed + 1 + i,
+                         degree=degree, name=f"batch{i}-{N}")
+        out.append(P)
+    return out
+
+
+FHN = dict(aode=0.5 * 0.01, bode=-1 * 0.01, code=0.0, vrest=0.1, vamp=1.0, vth=0.0, vpeak=1.0, c1ion=-1.0,
+           c2ion=0.0)
+
+
+def monodomain_problem(N: int = 512, alpha: float = 1.5, Kalpha: float = 1e-4, dt: float = 0.05, k: int = 10,
+                       m: int | None = None, C: int | None = None, tol: float | None = None):
+    """Fractional monodomain (FitzHugh-Nagumo) time loop of
+    problem_startup_monodomain.m:10-142 on an N x N Neumann grid over
+    [0, 2.5]^2: eta = Kalpha dt / dx^alpha, f1 = exp(-eta x^(alpha/2)) for the
+    solution column and f2 = phi(-eta x^(alpha/2)) for the reaction column,
+    the k smallest cosine modes deflated (phi = 1 on the zero mode), m from the
+    Krylov rule and C from the contour bound at tol = 1/N^2 unless given.
+    Returns (FabProblem with R = 2, dt, ode, FHN parameters)."""
+    tol = 1.0 / N ** 2 if tol is None else tol
+    A = problems.laplacian_2d(N, "N", 1.0)
+    lam, Q = problems.laplacian_2d_eigpairs(N, k, "N", 1.0)
+    l1 = float(lam.max())
+    lN = float(8 * math.sin((N - 1) * math.pi / (2 * N)) ** 2)
+    dx = 2.5 / (N - 1)
+    eta = Kalpha * dt / dx ** alpha
+    f1 = params.frac_exp(eta, alpha)
+
+    def f2(x):
+        x = np.asarray(x)
+        z = -eta * np.power(x, alpha / 2.0)
+        with np.errstate(invalid="ignore", divide="ignore"):
+            v = np.expm1(z) / z
+        return np.where(z == 0, 1.0, v)
+
+    if m is None:
+        m = params.krylov_dim([1.0], l1, lN, tol)
+    if C is None:
+        C = params.contour_size_from_bound(l1, lN, [f1, f2], tol)
+    g = np.linspace(0, 2.5, N)
+    X, Y = np.meshgrid(g, g)
+    ode = np.zeros_like(X)
+    xh = np.zeros_like(X)
+    ode[Y >= 1.25] = 0.1
+    xh[(X <= 1.25) & (Y < 1.25)] = 1.0
+    ode = ode.reshape(-1, order="F")
+    xh = xh.reshape(-1, order="F")
+    p = FHN
+    yh = p["c1ion"] / p["vamp"] ** 2 * xh * (xh - p["vrest"]) * (xh - p["vpeak"]) - ode
+    U = np.stack([xh, yh], axis=1)
+    P = make_problem(f"monodomain-{N}", A, U, Q, lam, [f1, f2], m, C, l1, lN, degree=0, prob_dim=2.0,
+                     meta=dict(N=N, alpha=alpha, Kalpha=Kalpha, dt=dt, eta=eta, k=k))
+    return P, dt, ode, dict(p)

@@ -121,6 +121,31 @@ void gm_default_args(gm_create_args* args);
  * Z = Q^T U, U <- U - Q Z, update = Q (f(lambda) o Z). */
 int gm_lanczos_create(const gm_create_args* args, gm_handle* out);
 
+/* One problem of a batch: its matrix, right-hand sides and method arrays
+ * (same meaning and layout as the fields of gm_create_args). */
+typedef struct gm_batch_problem {
+  int64_t n;
+  int format;
+  const int64_t* ptr;
+  const int64_t* ind;
+  const double* values;
+  const double* U;              /* n x nrhs */
+  const double* gamma;          /* gamma_size */
+  const double* gamma_s_real;   /* gamma_size x C */
+  const double* gamma_s_imag;
+  const double* wts;            /* nrhs blocks of C x 2 */
+  const double* shifts;         /* 2 m C nrhs */
+} gm_batch_problem;
+
+/* Several independent problems (uneven sizes allowed) in one engine: every
+ * launch runs all of them at once, each on its own group of blocks with its
+ * own barriers and reductions.  common supplies nrhs, subspace_size,
+ * gamma_size, contour_size, precision and the engine options; num_eigs must
+ * be 0.  Vectors (U, X, solution) are the problems' rows stacked in order
+ * (n = sum of n_p); aabb, Y and m_eff are per problem, in problem order.
+ * No counterpart in the reference (it runs one problem per engine). */
+int gm_batch_create(int nprob, const gm_batch_problem* probs, const gm_create_args* common, gm_handle* out);
+
 /* Replaces lanczos_delete (lanczos_delete.cpp:6-35). */
 int gm_lanczos_delete(gm_handle h);
 
@@ -187,6 +212,15 @@ int gm_solve(gm_handle h);
 /* End to end with host buffers: set_U(b_host), gm_solve, solution -> x_host. */
 int gm_solve_host(gm_handle h, const double* b_host, double* x_host);
 
+/* nsteps steps of the reference's time loop (nicksmethodgpu_problem.m:7-16,
+ * nicksmethodgpu_problem_monodomain.m:7-16): build_subspace + lin_sys_solves
+ * + apply_V fused, then update_U (mode 0, Fisher-KPP) or update_U_monodomain
+ * (mode 1, FitzHugh-Nagumo).  With use_graph = 1 the nsteps steps are
+ * captured once into a CUDA graph (cached per nsteps and mode) and replayed
+ * by a single graph launch.  Needs nrhs = 2; the last step's timing is
+ * phase slot [4] of gm_phase_times. */
+int gm_time_loop(gm_handle h, int nsteps, int mode, int use_graph);
+
 /* Waits for the handle's stream and returns the device status. */
 int gm_sync(gm_handle h);
 
@@ -201,11 +235,11 @@ int gm_phase_times(gm_handle h, float* ms5);
 
 /* Engine facts: [0] n, [1] nrhs, [2] m, [3] d, [4] C, [5] k, [6] precision,
  * [7] grid blocks, [8] threads per block, [9] SELL padded entries,
- * [10] device bytes held, [11] kernel launches so far. */
-int gm_info(gm_handle h, int64_t* info12);
+ * [10] device bytes held, [11] kernel launches so far, [12] problems. */
+int gm_info(gm_handle h, int64_t* info13);
 
-/* Effective Krylov dimension per RHS after the last build (< m after a
- * breakdown). */
+/* Effective Krylov dimension per (problem, RHS) after the last build (< m
+ * after a breakdown). */
 int gm_get_meff(gm_handle h, int* meff);
 
 /* Largest m * nrhs * C accepted by gm_lin_sys_solves_noalloc. */

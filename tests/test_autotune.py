@@ -1,0 +1,30 @@
+"""Autotuner search and cache logic (timing replaced by a model; no GPU)."""
+import json
+
+from gpumatfun_gb300 import autotune, workloads
+
+
+def test_tune_picks_fastest_and_caches(tmp_path):
+    P = workloads.config1_small(N=12, k=2, m=10, C=8, R=2)
+    calls = []
+
+    def fake(c):
+        calls.append(c)
+        return 1.0 + abs(c["threads"] - 256) / 256 + 0.5 * c["col_staging"] + 0.25 * c["sync_policy"] + 0.1 * c["blocks_per_sm"]
+
+    path = tmp_path / "tune.json"
+    r = autotune.tune(P, "mixed", cache_path=str(path), measure=fake)
+    assert r["threads"] == 256 and r["col_staging"] == 0 and r["sync_policy"] == 0 and r["blocks_per_sm"] == 0
+    assert not r["cached"] and r["trials"] == len(autotune.candidates(2)) == len(calls)
+    r2 = autotune.tune(P, "mixed", cache_path=str(path), measure=fake)
+    assert r2["cached"] and len(calls) == r["trials"]
+    assert json.loads(path.read_text())[autotune.signature(P, "mixed")]["threads"] == 256
+    # a different precision or workload is a different key
+    assert autotune.signature(P, "fp64") != autotune.signature(P, "mixed")
+    Q = workloads.config1_small(N=14, k=2, m=10, C=8, R=2)
+    assert autotune.signature(Q, "mixed") != autotune.signature(P, "mixed")
+
+
+def test_candidates_respect_rhs():
+    assert all(c["blocks_per_sm"] in (0, 1) for c in autotune.candidates(4))
+    assert {c["threads"] for c in autotune.candidates(1)} == {128, 256, 512}
