@@ -15,6 +15,7 @@
 
 #include "../../include/gpumatfun.h"
 #include "fab_kernel.cuh"
+#include "fe_kernels.cuh"
 
 using gm::KParams;
 
@@ -57,6 +58,19 @@ struct gm_engine {
   bool ev_used[5] = {};
   bool have_y = false, have_coef = false, have_V = false;
   bool capturing = false;        // launches are being recorded into a CUDA graph
+  int* csr2sell = nullptr;       // device: SELL slot of every stored entry (kept on request)
+  bool keep_map = false;
+  // finite-element structure for gm_fe_assemble / gm_fe_gradient
+  long long fe_ntri = 0;
+  long long* fe_ent_ptr = nullptr;
+  int* fe_ent_tri = nullptr;
+  double* fe_ent_coef = nullptr;
+  long long* fe_nodes = nullptr;
+  double* fe_kc = nullptr;
+  double2* fe_buf[6] = {};
+  long long* csr_ptr = nullptr;  // device CSR row pointer (kept with csr2sell)
+  double2* fe_yb = nullptr;
+  double2* fe_yg = nullptr;
   cudaGraphExec_t loop_exec = nullptr;
   int loop_steps = -1, loop_mode = -1;
   long long launches = 0;
@@ -231,6 +245,8 @@ int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp, const std:
   if (padded > 2147483647LL * 2) return fail(e, GM_ERR_UNSUPPORTED, "padded SELL size too large");
   std::vector<int> col(padded);
   std::vector<VT> val(padded);
+  std::vector<int> c2s;
+  if (e->keep_map) c2s.assign(A.ptr.back(), 0);
   for (long long s = 0; s < nsl; ++s) {
     const long long L = (off[s + 1] - off[s]) / 32;
     for (int l = 0; l < 32; ++l) {
@@ -239,6 +255,7 @@ int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp, const std:
       for (long long jj = 0; jj < L; ++jj) {
         const long long dst = off[s] + jj * 32 + l;
         if (jj < len) {
+          if (e->keep_map) c2s[A.ptr[r] + jj] = (int)dst;
           col[dst] = A.col[A.ptr[r] + jj];
           val[dst] = (VT)std::ldexp(A.val[A.ptr[r] + jj], -scale_exp);
         } else {
@@ -255,6 +272,8 @@ int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp, const std:
   if ((rc = dupload(e, &d_off, off.data(), off.size()))) return rc;
   if ((rc = dupload(e, &d_col, col.data(), col.size()))) return rc;
   if ((rc = dupload(e, &d_val, val.data(), val.size()))) return rc;
+  if (e->keep_map && (rc = dupload(e, &e->csr2sell, c2s.data(), c2s.size()))) return rc;
+  if (e->keep_map && (rc = dupload(e, &e->csr_ptr, A.ptr.data(), A.ptr.size()))) return rc;
   e->kp.slice_off = d_off;
   e->kp.col = d_col;
   e->kp.val = d_val;
@@ -521,6 +540,8 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
   }
   if (ntot > 2147483647LL) return fail(e, GM_ERR_UNSUPPORTED, "n above 2^31-1");
 
+  e->keep_map = a->keep_entry_map != 0 && np == 1;
+  if (a->keep_entry_map && probs[0].format != GM_CSR) return fail(e, GM_ERR_ARG, "keep_entry_map needs a CSR matrix");
   e->n = ntot; e->nprob = np; e->R = a->nrhs; e->m = a->subspace_size; e->d = a->gamma_size - 1;
   e->C = a->contour_size; e->k = a->num_eigs; e->prec = a->precision; e->sync_mode = a->sync_mode;
   e->threads = a->threads_per_block ? a->threads_per_block : 512;
@@ -862,6 +883,15 @@ int gm_get_solution(gm_handle h, double* dst) {
   return rc ? rc : check_sync(h);
 }
 
+int gm_get_solution_device(gm_handle h, double* dst_dev) {
+  if (!h || !dst_dev) return GM_ERR_ARG;
+  const long long total = h->n * h->R;
+  k_pack_out<<<(unsigned)((total + 255) / 256), 256, 0, h->stream>>>(h->kp.S, dst_dev, h->n, h->R);
+  GM_CUDA(h, cudaGetLastError());
+  h->launches++;
+  return h->sync_mode ? check_sync(h) : GM_OK;
+}
+
 int gm_get_aabb(gm_handle h, double* dst) {
   if (!h || !dst) return GM_ERR_ARG;
   GM_CUDA(h, cudaMemcpyAsync(dst, h->kp.aabb, (size_t)(h->m + 1) * 2 * h->R * h->nprob * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
@@ -933,6 +963,124 @@ int gm_solve_host(gm_handle h, const double* b_host, double* x_host) {
   rc = gm_solve(h);
   if (rc) return rc;
   return gm_get_solution(h, x_host);
+}
+
+int gm_fe_attach(gm_handle h, int64_t ntri, const int64_t* ent_ptr, const int32_t* ent_tri, const double* ent_coef,
+                 const int64_t* tri_nodes, const double* tri_kc) {
+  if (!h) return GM_ERR_ARG;
+  if (!h->csr2sell) return fail(h, GM_ERR_STATE, "fe_attach: create the engine with keep_entry_map = 1");
+  if (h->fe_ent_ptr) return fail(h, GM_ERR_STATE, "fe_attach: already attached");
+  if (ntri <= 0 || ntri > INT32_MAX) return fail(h, GM_ERR_ARG, "fe_attach: ntri out of range");
+  if (!ent_ptr || !ent_tri || !ent_coef || !tri_nodes || !tri_kc) return fail(h, GM_ERR_ARG, "fe_attach: null argument");
+  const long long nnz = h->nnz;
+  if (ent_ptr[0] != 0) return fail(h, GM_ERR_ARG, "fe_attach: ent_ptr[0] must be 0");
+  for (long long t = 0; t < nnz; ++t)
+    if (ent_ptr[t + 1] < ent_ptr[t]) return fail(h, GM_ERR_ARG, "fe_attach: ent_ptr not monotone");
+  const long long nc = ent_ptr[nnz];
+  for (long long p = 0; p < nc; ++p)
+    if (ent_tri[p] < 0 || ent_tri[p] >= ntri) return fail(h, GM_ERR_ARG, "fe_attach: triangle index out of range");
+  for (long long t = 0; t < 3 * ntri; ++t)
+    if (tri_nodes[t] < -1 || tri_nodes[t] >= h->n) return fail(h, GM_ERR_ARG, "fe_attach: node index out of range");
+  int rc;
+  h->fe_ntri = ntri;
+  if ((rc = dupload(h, &h->fe_ent_ptr, reinterpret_cast<const long long*>(ent_ptr), nnz + 1))) return rc;
+  if ((rc = dupload(h, &h->fe_ent_tri, ent_tri, nc))) return rc;
+  if ((rc = dupload(h, &h->fe_ent_coef, ent_coef, nc))) return rc;
+  if ((rc = dupload(h, &h->fe_nodes, reinterpret_cast<const long long*>(tri_nodes), 3 * ntri))) return rc;
+  if ((rc = dupload(h, &h->fe_kc, tri_kc, 9 * ntri))) return rc;
+  return GM_OK;
+}
+
+int gm_fe_assemble(gm_handle h, const double* kappa_dev) {
+  if (!h || !kappa_dev) return GM_ERR_ARG;
+  if (!h->fe_ent_ptr) return fail(h, GM_ERR_STATE, "fe_assemble before fe_attach");
+  const long long nnz = h->nnz;
+  const unsigned blocks = (unsigned)((nnz + 255) / 256);
+  if (h->prec == GM_FP64)
+    gm::k_fe_assemble<double><<<blocks, 256, 0, h->stream>>>(nnz, h->fe_ent_ptr, h->fe_ent_tri, h->fe_ent_coef, kappa_dev,
+                                                             h->csr2sell, (double*)h->kp.val, h->scale_exp);
+  else
+    gm::k_fe_assemble<float><<<blocks, 256, 0, h->stream>>>(nnz, h->fe_ent_ptr, h->fe_ent_tri, h->fe_ent_coef, kappa_dev,
+                                                            h->csr2sell, (float*)h->kp.val, h->scale_exp);
+  GM_CUDA(h, cudaGetLastError());
+  h->launches++;
+  h->have_V = h->have_y = h->have_coef = false;
+  return h->sync_mode ? check_sync(h) : GM_OK;
+}
+
+}  // extern "C"
+
+namespace {
+// Y -> the lift coefficients of the gradient: yb'[j][q] = y_b,j[q] / w_j
+// (w_j the true weight: the stored one times 2^se) and yg[j][q] = y_g,j[q].
+__global__ void k_fe_prep_y(int C, int m, const double* __restrict__ Yr, const double* __restrict__ Yi,
+                            const double* __restrict__ wts, int se, double2* __restrict__ yb, double2* __restrict__ yg) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= C * m) return;
+  const int j = t / m, q = t % m;
+  const double wr = ldexp(wts[j], se), wi = ldexp(wts[C + j], se);
+  const double ar = Yr[(long long)j * m + q], ai = Yi[(long long)j * m + q];
+  const double den = wr * wr + wi * wi;
+  yb[t] = make_double2((ar * wr + ai * wi) / den, (ai * wr - ar * wi) / den);
+  yg[t] = make_double2(Yr[(long long)(C + j) * m + q], Yi[(long long)(C + j) * m + q]);
+}
+}  // namespace
+
+extern "C" {
+
+int gm_fe_gradient(gm_handle h, double* dkappa_dev) {
+  if (!h || !dkappa_dev) return GM_ERR_ARG;
+  if (!h->fe_nodes) return fail(h, GM_ERR_STATE, "fe_gradient before fe_attach");
+  if (h->R != 2 || h->k != 0 || h->nprob != 1)
+    return fail(h, GM_ERR_UNSUPPORTED, "fe_gradient needs nrhs = 2 (b, g) and no deflation");
+  if (!h->have_y) return fail(h, GM_ERR_STATE, "fe_gradient needs build_subspace and lin_sys_solves for [b, g] first");
+  const long long n = h->n;
+  const int C = h->C, m = h->m, d = h->d;
+  int rc;
+  if (!h->fe_buf[0]) {
+    // Zb, Zg (lifts) and two Horner ping-pong pairs, each n x C complex
+    for (int t = 0; t < 6; ++t)
+      if ((rc = dalloc(h, &h->fe_buf[t], (size_t)n * C))) return rc;
+    if ((rc = dalloc(h, &h->fe_yb, (size_t)m * C))) return rc;
+    if ((rc = dalloc(h, &h->fe_yg, (size_t)m * C))) return rc;
+  }
+  double2 *Zb = h->fe_buf[0], *Zg = h->fe_buf[1];
+  double2 *Xb[2] = {h->fe_buf[2], h->fe_buf[3]}, *Xg[2] = {h->fe_buf[4], h->fe_buf[5]};
+  k_fe_prep_y<<<(C * m + 255) / 256, 256, 0, h->stream>>>(C, m, h->kp.Yr, h->kp.Yi, h->kp.wts, h->scale_exp,
+                                                           h->fe_yb, h->fe_yg);
+  const size_t smem = sizeof(double2) * 2 * 8 * m;
+  const unsigned lblocks = (unsigned)std::min<long long>((n + 255) / 256, 8LL * h->nsm);
+  if (h->prec == GM_FP64) {
+    if (smem > 48 * 1024)
+      GM_CUDA(h, cudaFuncSetAttribute(gm::k_fe_lift<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    gm::k_fe_lift<double><<<lblocks, 256, smem, h->stream>>>(n, m, C, (const double*)h->kp.V, h->fe_yb, h->fe_yg,
+                                                             Zb, Zg, h->kp.meff);
+  } else {
+    if (smem > 48 * 1024)
+      GM_CUDA(h, cudaFuncSetAttribute(gm::k_fe_lift<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    gm::k_fe_lift<float><<<lblocks, 256, smem, h->stream>>>(n, m, C, (const float*)h->kp.V, h->fe_yb, h->fe_yg,
+                                                            Zb, Zg, h->kp.meff);
+  }
+  h->launches += 2;
+  // X = gs(0, j) Z; X = A X + gs(i, j) Z for i = 1..d  ->  R_j, S_j
+  const unsigned hblocks = (unsigned)std::min<long long>((n + 7) / 8, 32LL * h->nsm);
+  for (int i = 0; i <= d; ++i) {
+    const int in = (i + 1) & 1, out = i & 1;
+    if (h->prec == GM_FP64)
+      gm::k_fe_horner<double><<<hblocks, 256, 0, h->stream>>>(n, C, d + 1, i, h->csr_ptr, h->csr2sell, h->kp.col,
+                                                              (const double*)h->kp.val, h->kp.gs_re, h->kp.gs_im, Zb, Zg,
+                                                              Xb[in], Xg[in], Xb[out], Xg[out], i == 0);
+    else
+      gm::k_fe_horner<float><<<hblocks, 256, 0, h->stream>>>(n, C, d + 1, i, h->csr_ptr, h->csr2sell, h->kp.col,
+                                                             (const float*)h->kp.val, h->kp.gs_re, h->kp.gs_im, Zb, Zg,
+                                                             Xb[in], Xg[in], Xb[out], Xg[out], i == 0);
+    h->launches++;
+  }
+  gm::k_fe_grad<<<(unsigned)((h->fe_ntri + 127) / 128), 128, 0, h->stream>>>(h->fe_ntri, C, h->fe_nodes, h->fe_kc,
+                                                                              Xb[d & 1], Xg[d & 1], dkappa_dev);
+  GM_CUDA(h, cudaGetLastError());
+  h->launches++;
+  return h->sync_mode ? check_sync(h) : GM_OK;
 }
 
 int gm_time_loop(gm_handle h, int nsteps, int mode, int use_graph) {

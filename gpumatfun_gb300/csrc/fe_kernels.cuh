@@ -1,0 +1,161 @@
+// Finite-element operator assembly and the adjoint (gradient) kernels.
+//
+// Operator: A(kappa) = M^{-1/2} K(kappa) M^{-1/2} on the interior nodes of a
+// P1 mesh, K(kappa) = sum_e kappa_e K_e with K_e the unit-coefficient element
+// stiffness (process_nonuniform.m:90-91 forms the same symmetric scaling).
+//
+// Adjoint of L = 1/2 ||f(A) b - d||^2 (g = f(A) b - d), from the contour form
+// f(A) = Im sum_j w_j (xi_j - A)^{-1} (Frechet derivative of the resolvent):
+//   dL/db       = f(A) g
+//   dL/dkappa_e = Im sum_j w_j s_j^T (dA/dkappa_e) r_j,
+//   r_j = (xi_j - A)^{-1} b,  s_j = (xi_j - A)^{-1} g.
+// With the polynomial preconditioner p, B = A p(A), sigma_j = xi_j p(xi_j) and
+// q_j(x) = (sigma_j - x p(x)) / (xi_j - x) = sum_i gs(i, j) x^(d-i):
+//   (xi_j - A)^{-1} = q_j(A) (sigma_j - B)^{-1},
+// and the engine's shifted solves give V y_j = w_j (sigma_j - B)^{-1} u for
+// right-hand side u.  Hence
+//   dL/dkappa_e = Im sum_j S_j^T dA_e R_j,
+//   R_j = q_j(A) V_b (y_b,j / w_j),  S_j = q_j(A) V_g y_g,j,
+// evaluated as one lift Z = V y per side (n x C complex) and d Horner steps
+// X <- A X + gs(i, j) Z.  dA_e is local to the triangle's three nodes:
+// (dA_e)_{ac} = msi_a K_e[a][c] msi_c.
+#pragma once
+#include "fab_kernel.cuh"
+
+namespace gm {
+
+// value of every stored entry of A from kappa, in a fixed order (no atomics):
+// val[slot[t]] = 2^-se sum_{p in ent_ptr[t]..} kappa[ent_tri[p]] * ent_coef[p]
+template <class VT>
+__global__ void k_fe_assemble(long long nnz, const long long* __restrict__ ent_ptr, const int* __restrict__ ent_tri,
+                              const double* __restrict__ ent_coef, const double* __restrict__ kappa,
+                              const int* __restrict__ slot, VT* __restrict__ val, int se) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nnz) return;
+  double acc = 0.0;
+  for (long long p = ent_ptr[t]; p < ent_ptr[t + 1]; ++p) acc = fma(kappa[ent_tri[p]], ent_coef[p], acc);
+  val[slot[t]] = (VT)ldexp(acc, -se);
+}
+
+// Zb[i][j] = sum_q V[q][i][0] yb'[j][q], Zg[i][j] = sum_q V[q][i][1] yg[j][q]
+// (complex; yb' = y_b / w); rows by thread, shifts in chunks of JC whose
+// coefficients sit in shared memory.
+template <class BT>
+__global__ void k_fe_lift(long long n, int m, int C, const BT* __restrict__ V, const double2* __restrict__ yb,
+                          const double2* __restrict__ yg, double2* __restrict__ Rout, double2* __restrict__ Sout,
+                          const int* __restrict__ meff) {
+  constexpr int JC = 8;
+  extern __shared__ double2 sy[];  // [2][JC][m]
+  const int mb = min(meff[0], m), mg = min(meff[1], m);
+  for (int j0 = 0; j0 < C; j0 += JC) {
+    __syncthreads();
+    for (int t = threadIdx.x; t < 2 * JC * m; t += blockDim.x) {
+      const int side = t / (JC * m), rest = t % (JC * m), jj = rest / m, q = rest % m;
+      const int j = j0 + jj;
+      const double2* src = side ? yg : yb;
+      sy[t] = (j < C) ? src[(long long)j * m + q] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+      double2 ra[JC], sa[JC];
+#pragma unroll
+      for (int jj = 0; jj < JC; ++jj) { ra[jj] = make_double2(0.0, 0.0); sa[jj] = make_double2(0.0, 0.0); }
+      for (int q = 0; q < m; ++q) {
+        const double vb = q < mb ? (double)V[((long long)q * n + i) * 2] : 0.0;
+        const double vg = q < mg ? (double)V[((long long)q * n + i) * 2 + 1] : 0.0;
+#pragma unroll
+        for (int jj = 0; jj < JC; ++jj) {
+          const double2 b = sy[jj * m + q];
+          const double2 g = sy[JC * m + jj * m + q];
+          ra[jj].x = fma(vb, b.x, ra[jj].x);
+          ra[jj].y = fma(vb, b.y, ra[jj].y);
+          sa[jj].x = fma(vg, g.x, sa[jj].x);
+          sa[jj].y = fma(vg, g.y, sa[jj].y);
+        }
+      }
+#pragma unroll
+      for (int jj = 0; jj < JC; ++jj) {
+        if (j0 + jj < C) {
+          Rout[i * C + j0 + jj] = ra[jj];
+          Sout[i * C + j0 + jj] = sa[jj];
+        }
+      }
+    }
+  }
+}
+
+// Xout[r][j] = sum_k A[r][k] Xin[k][j] + gs(i, j) Z[r][j] for both sides
+// (first step: gs(0, j) Z[r][j] only).  One warp per row, lanes over the
+// shifts j, so every stored entry of the row reads one contiguous
+// C-vector of X.  A's entries are read through the CSR-entry -> slot map.
+template <class VT>
+__global__ void k_fe_horner(long long n, int C, int d1, int i, const long long* __restrict__ ptr,
+                            const int* __restrict__ c2s, const int* __restrict__ col, const VT* __restrict__ val,
+                            const double* __restrict__ gs_re, const double* __restrict__ gs_im,
+                            const double2* __restrict__ Zb, const double2* __restrict__ Zg,
+                            const double2* __restrict__ Xb, const double2* __restrict__ Xg,
+                            double2* __restrict__ Yb, double2* __restrict__ Yg, int first) {
+  const int lane = threadIdx.x & 31;
+  const long long nwarps = (long long)gridDim.x * (blockDim.x >> 5);
+  for (long long r = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); r < n; r += nwarps) {
+    for (int j = lane; j < C; j += 32) {
+      double2 ab = make_double2(0.0, 0.0), ag = make_double2(0.0, 0.0);
+      if (!first) {
+        for (long long t = ptr[r]; t < ptr[r + 1]; ++t) {
+          const int s = c2s[t];
+          const long long k = col[s];
+          const double v = (double)val[s];
+          const double2 xb = Xb[k * C + j], xg = Xg[k * C + j];
+          ab.x = fma(v, xb.x, ab.x);
+          ab.y = fma(v, xb.y, ab.y);
+          ag.x = fma(v, xg.x, ag.x);
+          ag.y = fma(v, xg.y, ag.y);
+        }
+      }
+      const double gr = gs_re[i + (long long)d1 * j], gi = gs_im[i + (long long)d1 * j];
+      const double2 zb = Zb[r * C + j], zg = Zg[r * C + j];
+      ab.x += gr * zb.x - gi * zb.y;
+      ab.y += gr * zb.y + gi * zb.x;
+      ag.x += gr * zg.x - gi * zg.y;
+      ag.y += gr * zg.y + gi * zg.x;
+      Yb[r * C + j] = ab;
+      Yg[r * C + j] = ag;
+    }
+  }
+}
+
+// dkappa[e] = Im sum_j sum_{a,c} S[n_a][j] Kc_e[a][c] R[n_c][j]  (one thread
+// per triangle; boundary nodes (index -1) contribute nothing)
+__global__ void k_fe_grad(long long ntri, int C, const long long* __restrict__ nodes, const double* __restrict__ kc,
+                          const double2* __restrict__ R, const double2* __restrict__ S, double* __restrict__ dk) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= ntri) return;
+  long long nd[3];
+  double K[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) nd[a] = nodes[e * 3 + a];
+#pragma unroll
+  for (int t = 0; t < 9; ++t) K[t] = kc[e * 9 + t];
+  double acc = 0.0;
+  for (int j = 0; j < C; ++j) {
+    double2 r[3], s[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      r[a] = nd[a] >= 0 ? R[nd[a] * C + j] : make_double2(0.0, 0.0);
+      s[a] = nd[a] >= 0 ? S[nd[a] * C + j] : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      double tr = 0.0, ti = 0.0;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        tr = fma(K[a * 3 + c], r[c].x, tr);
+        ti = fma(K[a * 3 + c], r[c].y, ti);
+      }
+      acc = fma(s[a].x, ti, fma(s[a].y, tr, acc));  // Im(s_a * t_a)
+    }
+  }
+  dk[e] = acc;
+}
+
+}  // namespace gm

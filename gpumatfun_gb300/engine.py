@@ -33,7 +33,8 @@ EXPORTED_SYMBOLS = [
     "gm_get_xsol", "gm_get_aabb", "gm_set_y", "gm_get_y", "gm_set_U", "gm_set_U_device", "gm_get_update",
     "gm_get_solution", "gm_solve", "gm_solve_host", "gm_sync", "gm_set_stream",
     "gm_phase_times", "gm_info", "gm_get_meff", "gm_last_error", "gm_version",
-    "gm_lin_sys_solves_noalloc", "gm_batch_create", "gm_time_loop",
+    "gm_lin_sys_solves_noalloc", "gm_batch_create", "gm_time_loop", "gm_fe_attach", "gm_fe_assemble",
+    "gm_fe_gradient", "gm_get_solution_device",
 ]
 
 _dp = ct.POINTER(ct.c_double)
@@ -58,7 +59,7 @@ class CreateArgs(ct.Structure):
         ("precision", ct.c_int), ("sync_mode", ct.c_int), ("threads_per_block", ct.c_int),
         ("blocks_per_sm", ct.c_int), ("sell_sigma", ct.c_int),
         ("barrier_timeout_s", ct.c_double), ("breakdown_tol", ct.c_double),
-        ("sync_policy", ct.c_int), ("col_staging", ct.c_int),
+        ("sync_policy", ct.c_int), ("col_staging", ct.c_int), ("keep_entry_map", ct.c_int),
     ]
 
 
@@ -103,6 +104,10 @@ def load_library(build_if_missing: bool = False) -> ct.CDLL:
     lib.gm_solve_host.argtypes = [h, _dp, _dp]
     lib.gm_set_stream.argtypes = [h, ct.c_void_p]
     lib.gm_time_loop.argtypes = [h, ct.c_int, ct.c_int, ct.c_int]
+    lib.gm_fe_attach.argtypes = [h, ct.c_int64, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]
+    lib.gm_fe_assemble.argtypes = [h, ct.c_void_p]
+    lib.gm_fe_gradient.argtypes = [h, ct.c_void_p]
+    lib.gm_get_solution_device.argtypes = [h, ct.c_void_p]
     lib.gm_phase_times.argtypes = [h, ct.POINTER(ct.c_float)]
     lib.gm_info.argtypes = [h, _lp]
     lib.gm_get_meff.argtypes = [h, ct.POINTER(ct.c_int)]
@@ -111,6 +116,9 @@ def load_library(build_if_missing: bool = False) -> ct.CDLL:
     lib.gm_version.restype = ct.c_char_p
     _LIB = lib
     return lib
+
+
+STREAM_LEGACY = 1  # cudaStreamLegacy
 
 
 class GmError(RuntimeError):
@@ -135,7 +143,7 @@ class Engine:
                  precision: str | int = "fp64", sync: bool = True, threads: int = 0,
                  blocks_per_sm: int = 0, sell_sigma: int = 0, timeout_s: float = 0.0,
                  breakdown_tol: float = 0.0, matrix_format: str = "csr", sync_policy: int = 0,
-                 col_staging: int = 0):
+                 col_staging: int = 0, keep_entry_map: bool = False):
         self._lib = load_library()
         self._h = ct.c_void_p()
         n = A.shape[0]
@@ -189,6 +197,7 @@ class Engine:
         a.barrier_timeout_s, a.breakdown_tol = timeout_s, breakdown_tol
         a.sync_policy = int(sync_policy)
         a.col_staging = int(col_staging)
+        a.keep_entry_map = 1 if keep_entry_map else 0
         self._keep = (ptr, ind, val, U, Q, lam, flam, gamma, gs_re, gs_im, wts, shifts, cs, mass, ode)
         rc = self._lib.gm_lanczos_create(ct.byref(a), ct.byref(self._h))
         self._keep = None
@@ -270,6 +279,25 @@ class Engine:
     def get_solution(self) -> np.ndarray:
         return self._out(self._lib.gm_get_solution)
 
+    def get_solution_device(self, ptr: int):
+        """Solution (column-major n x nrhs FP64) into device memory at ``ptr``."""
+        self._check(self._lib.gm_get_solution_device(self._h, ct.c_void_p(ptr)))
+
+    def fe_attach(self, ntri: int, ent_ptr, ent_tri, ent_coef, tri_nodes, tri_kc):
+        """Finite-element structure of A(kappa) (engine created with
+        keep_entry_map=True from a CSR matrix); see gm_fe_attach."""
+        arrs = (np.ascontiguousarray(ent_ptr, dtype=np.int64), np.ascontiguousarray(ent_tri, dtype=np.int32),
+                _f64(ent_coef), np.ascontiguousarray(tri_nodes, dtype=np.int64), _f64(tri_kc))
+        self._check(self._lib.gm_fe_attach(self._h, int(ntri), *[a.ctypes.data_as(ct.c_void_p) for a in arrs]))
+
+    def fe_assemble(self, kappa_ptr: int):
+        """A <- A(kappa), kappa a device pointer to ntri doubles."""
+        self._check(self._lib.gm_fe_assemble(self._h, ct.c_void_p(kappa_ptr)))
+
+    def fe_gradient(self, dkappa_ptr: int):
+        """dL/dkappa (device pointer, ntri doubles) after solving for U = [b, g]."""
+        self._check(self._lib.gm_fe_gradient(self._h, ct.c_void_p(dkappa_ptr)))
+
     def get_update(self) -> np.ndarray:
         return self._out(self._lib.gm_get_update)
 
@@ -291,7 +319,16 @@ class Engine:
         self._check(self._lib.gm_sync(self._h))
 
     def set_stream(self, stream_ptr: int | None):
-        self._check(self._lib.gm_set_stream(self._h, ct.c_void_p(stream_ptr or 0)))
+        """Launch on an external stream.  None restores the handle's own stream;
+        0 (the legacy default stream, e.g. torch's default stream) is passed
+        as CUDA's cudaStreamLegacy handle so that it is not taken for None."""
+        if stream_ptr is None:
+            handle = 0
+        elif stream_ptr == 0:
+            handle = STREAM_LEGACY
+        else:
+            handle = stream_ptr
+        self._check(self._lib.gm_set_stream(self._h, ct.c_void_p(handle)))
 
     def phase_times(self) -> dict:
         ms = (ct.c_float * 5)()

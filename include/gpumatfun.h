@@ -110,6 +110,8 @@ typedef struct gm_create_args {
                                   1 = grid barriers                               */
   int col_staging;             /* 0 = stage SELL column indices in shared memory by
                                   TMA bulk copies (default), 1 = read them directly */
+  int keep_entry_map;          /* 1 = keep the map from stored entries (CSR order)
+                                  to device slots, needed by gm_fe_attach          */
 } gm_create_args;
 
 /* Fill *args with defaults (zeros, struct_version, sync_mode = 1, nrhs = 2). */
@@ -205,12 +207,42 @@ int gm_get_update(gm_handle h, double* dst);
 /* f(A) b for every column: X + update (n x nrhs, column-major) to dst. */
 int gm_get_solution(gm_handle h, double* dst);
 
+/* The same solution, column-major n x nrhs, into device memory on the
+ * handle's stream (no host synchronisation unless sync_mode is set). */
+int gm_get_solution_device(gm_handle h, double* dst_dev);
+
 /* One f(A)b evaluation in a single persistent launch: build_subspace,
  * lin_sys_solves and apply_V fused; then X + update is available. */
 int gm_solve(gm_handle h);
 
 /* End to end with host buffers: set_U(b_host), gm_solve, solution -> x_host. */
 int gm_solve_host(gm_handle h, const double* b_host, double* x_host);
+
+/* Finite-element operator A(kappa) = M^{-1/2} K(kappa) M^{-1/2}, K(kappa) =
+ * sum_e kappa_e K_e (unit-coefficient P1 element stiffness K_e), for the
+ * adjoint of fractional diffusion.  No counterpart in the reference (its
+ * matrices are fixed inputs).  The engine must be created from a CSR matrix
+ * with keep_entry_map = 1.
+ *   ent_ptr  (nnz+1) : for stored entry t (CSR order) of A, its contributions
+ *   ent_tri, ent_coef: are kappa[ent_tri[p]] * ent_coef[p], p in ent_ptr[t]..
+ *   tri_nodes (ntri x 3): row of each vertex, -1 for a boundary vertex
+ *   tri_kc   (ntri x 9): msi_a K_e[a][c] msi_c (row-major), msi = M^{-1/2}  */
+int gm_fe_attach(gm_handle h, int64_t ntri, const int64_t* ent_ptr, const int32_t* ent_tri, const double* ent_coef,
+                 const int64_t* tri_nodes, const double* tri_kc);
+
+/* Recomputes A's stored values from kappa (device pointer, ntri doubles) on
+ * the handle's stream; Krylov state is invalidated. */
+int gm_fe_assemble(gm_handle h, const double* kappa_dev);
+
+/* dL/dkappa (device pointer, ntri doubles) for L = 1/2 ||f(A) b - d||^2, after
+ * a solve (gm_solve, or build_subspace + lin_sys_solves) with U = [b, g],
+ * g = f(A) b - d (nrhs = 2, both columns with the weights of f, no deflation):
+ *   dL/dkappa_e = Im sum_j w_j s_j^T (M^{-1/2} K_e M^{-1/2}) r_j,
+ *   r_j = (xi_j - A)^{-1} b,  s_j = (xi_j - A)^{-1} g,
+ * with (xi_j - A)^{-1} = q_j(A) (sigma_j - A p(A))^{-1} from the engine's
+ * shifted solves (q_j the shifted polynomial, gamma_s(:, j)).
+ * dL/db = f(A) g is column 1 of the solution. */
+int gm_fe_gradient(gm_handle h, double* dkappa_dev);
 
 /* nsteps steps of the reference's time loop (nicksmethodgpu_problem.m:7-16,
  * nicksmethodgpu_problem_monodomain.m:7-16): build_subspace + lin_sys_solves
@@ -225,7 +257,9 @@ int gm_time_loop(gm_handle h, int nsteps, int mode, int use_graph);
 int gm_sync(gm_handle h);
 
 /* Uses an external CUDA stream (cudaStream_t passed as void*); NULL restores
- * the handle's own stream. */
+ * the handle's own stream.  The legacy default stream (the stream PyTorch's
+ * default stream is) is selected by its CUDA handle value, cudaStreamLegacy
+ * ((void*)1); cudaStreamPerThread ((void*)2) likewise. */
 int gm_set_stream(gm_handle h, void* stream);
 
 /* Device milliseconds of the last launch of each phase group, measured with
