@@ -59,6 +59,10 @@ struct gm_engine {
   bool have_y = false, have_coef = false, have_V = false;
   bool capturing = false;        // launches are being recorded into a CUDA graph
   int* csr2sell = nullptr;       // device: SELL slot of every stored entry (kept on request)
+  void* mat_base = nullptr;      // SELL values + column indices (one allocation)
+  size_t mat_bytes = 0;
+  bool l2_window = false;        // launches carry an L2 persisting window over the matrix
+  cudaAccessPolicyWindow window = {};
   bool keep_map = false;
   // finite-element structure for gm_fe_assemble / gm_fe_gradient
   long long fe_ntri = 0;
@@ -266,12 +270,22 @@ int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp, const std:
     }
   }
   long long* d_off;
-  int* d_col;
-  VT* d_val;
   int rc;
   if ((rc = dupload(e, &d_off, off.data(), off.size()))) return rc;
-  if ((rc = dupload(e, &d_col, col.data(), col.size()))) return rc;
-  if ((rc = dupload(e, &d_val, val.data(), val.size()))) return rc;
+  // values and column indices in one allocation, so that one L2 access-policy
+  // window can cover the whole matrix
+  const size_t vbytes = ((size_t)padded * sizeof(VT) + 255) & ~(size_t)255;
+  const size_t mbytes = vbytes + (size_t)padded * sizeof(int);
+  unsigned char* d_mat;
+  if ((rc = dalloc(e, &d_mat, mbytes))) return rc;
+  VT* d_val = reinterpret_cast<VT*>(d_mat);
+  int* d_col = reinterpret_cast<int*>(d_mat + vbytes);
+  if (padded) {
+    GM_CUDA(e, cudaMemcpy(d_val, val.data(), (size_t)padded * sizeof(VT), cudaMemcpyHostToDevice));
+    GM_CUDA(e, cudaMemcpy(d_col, col.data(), (size_t)padded * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  e->mat_base = d_mat;
+  e->mat_bytes = mbytes;
   if (e->keep_map && (rc = dupload(e, &e->csr2sell, c2s.data(), c2s.size()))) return rc;
   if (e->keep_map && (rc = dupload(e, &e->csr_ptr, A.ptr.data(), A.ptr.size()))) return rc;
   e->kp.slice_off = d_off;
@@ -451,11 +465,16 @@ int launch(gm_engine* e, int phases, int slot) {
   cfg.blockDim = dim3(e->threads);
   cfg.dynamicSmemBytes = e->smem[grp];
   cfg.stream = e->stream;
-  cudaLaunchAttribute attr[1];
+  cudaLaunchAttribute attr[2];
   attr[0].id = cudaLaunchAttributeCooperative;
   attr[0].val.cooperative = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
+  if (e->l2_window) {
+    attr[1].id = cudaLaunchAttributeAccessPolicyWindow;
+    attr[1].val.accessPolicyWindow = e->window;
+    cfg.numAttrs = 2;
+  }
   cudaError_t st = cudaLaunchKernelExC(&cfg, e->kfn[grp], args);
   if (st != cudaSuccess) return cuda_fail(e, st, "cooperative launch");
   e->launches++;
@@ -499,6 +518,7 @@ int set_usol(gm_engine* e, const double* U, bool on_device) {
 void destroy(gm_engine* e) {
   if (!e) return;
   if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->l2_window) cudaCtxResetPersistingL2Cache();
   if (e->loop_exec) cudaGraphExecDestroy(e->loop_exec);
   for (auto& b : e->bufs) cudaFree(b.p);
   e->bufs.clear();
@@ -622,6 +642,25 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
   if ((rc = build_partition(e, csr, slot_rows, slice_off, pslice0, prow0))) return rc;
   e->kp.dep_mode = a->sync_policy == 0 ? 1 : 0;
   csr = Csr();
+  if (a->l2_window == 0 && e->mat_bytes > 0) {
+    // Persisting L2 lines for the matrix, which every SpMV pass re-reads: the
+    // set-aside is this context's (released with it); the hit ratio spreads
+    // the limit over the window when the matrix is larger than the limit.
+    int max_persist = 0, max_window = 0;
+    GM_CUDA(e, cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, e->dev));
+    GM_CUDA(e, cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, e->dev));
+    if (max_persist > 0 && max_window > 0) {
+      const size_t win = std::min<size_t>(e->mat_bytes, (size_t)max_window);
+      const size_t setaside = std::min<size_t>(win, (size_t)max_persist);
+      GM_CUDA(e, cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, setaside));
+      e->window.base_ptr = e->mat_base;
+      e->window.num_bytes = win;
+      e->window.hitRatio = (float)std::min(1.0, (double)setaside / (double)win);
+      e->window.hitProp = cudaAccessPropertyPersisting;
+      e->window.missProp = cudaAccessPropertyStreaming;
+      e->l2_window = true;
+    }
+  }
 
   KParams& kp = e->kp;
   const long long n = e->n;

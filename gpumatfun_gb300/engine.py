@@ -60,6 +60,7 @@ class CreateArgs(ct.Structure):
         ("blocks_per_sm", ct.c_int), ("sell_sigma", ct.c_int),
         ("barrier_timeout_s", ct.c_double), ("breakdown_tol", ct.c_double),
         ("sync_policy", ct.c_int), ("col_staging", ct.c_int), ("keep_entry_map", ct.c_int),
+        ("l2_window", ct.c_int),
     ]
 
 
@@ -143,7 +144,7 @@ class Engine:
                  precision: str | int = "fp64", sync: bool = True, threads: int = 0,
                  blocks_per_sm: int = 0, sell_sigma: int = 0, timeout_s: float = 0.0,
                  breakdown_tol: float = 0.0, matrix_format: str = "csr", sync_policy: int = 0,
-                 col_staging: int = 0, keep_entry_map: bool = False):
+                 col_staging: int = 0, keep_entry_map: bool = False, l2_window: int = 0):
         self._lib = load_library()
         self._h = ct.c_void_p()
         n = A.shape[0]
@@ -198,6 +199,7 @@ class Engine:
         a.sync_policy = int(sync_policy)
         a.col_staging = int(col_staging)
         a.keep_entry_map = 1 if keep_entry_map else 0
+        a.l2_window = int(l2_window)
         self._keep = (ptr, ind, val, U, Q, lam, flam, gamma, gs_re, gs_im, wts, shifts, cs, mass, ode)
         rc = self._lib.gm_lanczos_create(ct.byref(a), ct.byref(self._h))
         self._keep = None

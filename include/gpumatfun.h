@@ -112,6 +112,9 @@ typedef struct gm_create_args {
                                   TMA bulk copies (default), 1 = read them directly */
   int keep_entry_map;          /* 1 = keep the map from stored entries (CSR order)
                                   to device slots, needed by gm_fe_attach          */
+  int l2_window;               /* 0 = launches keep the SELL matrix resident in L2
+                                  (persisting access-policy window, up to the
+                                  device's persisting limit; default), 1 = off     */
 } gm_create_args;
 
 /* Fill *args with defaults (zeros, struct_version, sync_mode = 1, nrhs = 2). */
