@@ -367,8 +367,228 @@ def mixed_batched(P, K, W, dev, stream, x_ref_engine=None):
             "note": "fused launch only (b resident, deflation excluded); same b for both precisions"}
 
 
+def run_adjoint(args):
+    """Adjoint workload: x = f(A(kappa)) b on the 250k-node FE disk, loss
+    L = 1/2 ||x - d||^2, one step = forward + backward (dL/dkappa per
+    triangle and dL/db) through the same calls torch.autograd uses."""
+    import torch
+    from gpumatfun_gb300 import adjoint, workloads
+    n_target = int(args.workload.split("-")[-1].replace("k", "000"))
+    K, W = args.steps, args.warmup
+    t0 = time.perf_counter()
+    mesh, kappa, kstar, b = workloads.adjoint_case(n_target)
+    prm = dict(workloads.ADJOINT_PARAMS)
+    out = {}
+    ops = {}
+    for prec in ("fp64", "mixed"):
+        ops[prec] = adjoint.FracFEOperator(mesh, kappa, precision=prec, **prm)
+    setup_s = time.perf_counter() - t0
+    op = ops["fp64"]
+    dev = torch.device("cuda", 0)
+    kt = torch.as_tensor(kappa, device=dev)
+    bt = torch.as_tensor(b, device=dev)
+    xs = op.forward(torch.as_tensor(kstar, device=dev), bt)
+    gen = torch.Generator(device=dev).manual_seed(5)
+    noise = torch.randn(xs.shape, generator=gen, device=dev, dtype=torch.float64)
+    d = xs + 0.01 * xs.norm() / xs.numel() ** 0.5 * noise
+    grads = {}
+    for prec, o in ops.items():
+        for _ in range(W):
+            x = o.forward(kt, bt)
+            o.backward(kt, bt, x - d)
+        torch.cuda.synchronize()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        tf = tb = 0.0
+        for _ in range(K):
+            e[0].record()
+            x = o.forward(kt, bt)
+            g = x - d
+            e[1].record()
+            dk, db = o.backward(kt, bt, g)
+            e[2].record()
+            torch.cuda.synchronize()
+            tf += e[0].elapsed_time(e[1])
+            tb += e[1].elapsed_time(e[2])
+        grads[prec] = (dk.cpu().numpy(), db.cpu().numpy(), x.cpu().numpy())
+        out[prec] = {"grad_evals_per_s": 1e3 * K / (tf + tb), "forward_ms": tf / K, "backward_ms": tb / K}
+    # end to end with host buffers (numpy in, numpy out), FP64
+    kh, bh = np.ascontiguousarray(kappa), np.ascontiguousarray(b)
+    dh = d.cpu().numpy()
+    xh = np.empty_like(bh)
+    dkh = np.empty(op.ntri)
+    dbh = np.empty_like(bh)
+    op.engine.set_stream(None)
+    t1 = time.perf_counter()
+    for _ in range(K):
+        op.engine.fe_forward(kh.ctypes.data, bh.ctypes.data, xh.ctypes.data)
+        gh = xh - dh
+        op.engine.fe_backward(kh.ctypes.data, bh.ctypes.data, gh.ctypes.data, dkh.ctypes.data, dbh.ctypes.data)
+    e2e_s = (time.perf_counter() - t1) / K
+    op._stream = None
+    dk64, db64, x64 = grads["fp64"]
+    dkm, dbm, xm = grads["mixed"]
+    rel = lambda a, r: float(np.linalg.norm(a - r) / np.linalg.norm(r))
+    # central finite differences of the FP64 loss on 64 random directions
+    # v = kappa * N(0, 1) per triangle, at the step 1e-6 and at 1e-3; the
+    # rounding noise of the loss itself is measured by perturbing kappa by
+    # 1e-14 relative, and bounds what the small step can resolve (noise / h).
+    def loss(k):
+        xx = op.forward(k, bt)
+        return 0.5 * float(torch.sum((xx - d) ** 2))
+    dkt = torch.as_tensor(dk64, device=dev)
+    L0 = loss(kt)
+    noise = max(abs(loss(kt * (1 + 1e-14 * torch.randn(kt.shape, generator=gen, device=dev,
+                                                            dtype=torch.float64))) - L0) for _ in range(3))
+    dirs = [kt * torch.randn(kt.shape, generator=gen, device=dev, dtype=torch.float64) for _ in range(64)]
+    ads = np.array([float(torch.dot(dkt, v)) for v in dirs])
+    t2 = time.perf_counter()
+    fd_out = {}
+    for h in (1e-6, 1e-3):
+        fds = np.array([(loss(kt + h * v) - loss(kt - h * v)) / (2 * h) for v in dirs])
+        err = np.abs(fds - ads) / np.sqrt(np.mean(ads ** 2))
+        fd_out[f"h={h:g}"] = {"max_err": float(err.max()), "median_err": float(np.median(err)),
+                              "noise_bound": float(noise / h / np.sqrt(np.mean(ads ** 2)))}
+    fd_out.update({"directions": 64, "loss": L0, "loss_noise": noise,
+                   "err": "|FD - adjoint| / rms(adjoint) over the directions; noise_bound = loss_noise / h "
+                          "in the same units", "seconds": time.perf_counter() - t2})
+    line = {"metric": "adjoint gradient evaluations/s (forward + backward: dL/dkappa per triangle and dL/db)",
+            "value": out["fp64"]["grad_evals_per_s"], "unit": "grad-evals/s", "n_gpus": 1, "steps": K, "warmup": W,
+            "ms_per_step": out["fp64"]["forward_ms"] + out["fp64"]["backward_ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded disk mesh, two Gaussian-field coefficients kappa and kappa*, uniform b, "
+                    "d = f(A(kappa*)) b + 1% noise)",
+            "config": {"workload": args.workload, "n": int(op.n), "ntri": int(op.ntri), **prm,
+                       "l1": op.l1, "lN": op.lN},
+            "e2e": {"value": 1.0 / e2e_s, "unit": "grad-evals/s", "h2d_bytes_per_step": 8 * (2 * op.ntri + 3 * op.n),
+                    "d2h_bytes_per_step": 8 * (op.ntri + 2 * op.n)},
+            "fp64": out["fp64"], "mixed": out["mixed"],
+            "mixed_vs_fp64": {"x": rel(xm, x64), "dL_dkappa": rel(dkm, dk64), "dL_db": rel(dbm, db64)},
+            "finite_differences": fd_out,
+            "setup_s": setup_s}
+    for o in ops.values():
+        o.delete()
+    print(json.dumps(line), flush=True)
+
+
+def _timed_solves(eng, stream, K, W):
+    """Median-free device time of K back-to-back fused solves on ``stream`` (ms per solve)."""
+    import torch
+    eng.set_stream(stream.cuda_stream)
+    with torch.cuda.stream(stream):
+        for _ in range(max(1, W)):
+            eng.solve()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(K):
+            eng.solve()
+        e1.record(stream)
+        torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / K
+
+
+def run_batch(args):
+    """Batched serving-style workload: 64 fractional-diffusion problems of
+    uneven size (N^2 grids, N log-uniform in [64, 1024]), 4 right-hand sides
+    each, one persistent launch; against the plain FP64 single-solve engine
+    (one problem, one right-hand side per launch) on the same 256 solves.
+    Plus the fractional monodomain time loop (512^2, 200 steps, CUDA graph)."""
+    import torch
+    from gpumatfun_gb300 import BatchEngine, Engine, LanczosEngine, workloads
+    K, W = args.steps, args.warmup
+    t0 = time.perf_counter()
+    probs = workloads.config5_batch()
+    setup_s = time.perf_counter() - t0
+    nsolves = sum(P.R for P in probs)
+    stream = torch.cuda.Stream()
+    res, sols = {}, {}
+    for prec in ("mixed", "fp64"):
+        eng = BatchEngine(probs, precision=prec, sync=False)
+        ms = _timed_solves(eng, stream, K, W)
+        sols[prec] = eng.split(eng.get_solution())
+        res[prec] = {"ms_per_launch": ms, "solves_per_s": nsolves * 1e3 / ms, "grid_blocks": eng.info()["grid_blocks"],
+                     "device_bytes": eng.info()["device_bytes"]}
+        if prec == "mixed":
+            # end to end: host right-hand sides in, host solutions out, every step
+            Uh = np.ascontiguousarray(np.concatenate([P.U for P in probs]))
+            eng.set_stream(None)
+            eng.set_U(Uh); eng.solve(); eng.get_solution()
+            t1 = time.perf_counter()
+            for _ in range(K):
+                eng.set_U(Uh)
+                eng.solve()
+                eng.get_solution()
+            e2e_ms = (time.perf_counter() - t1) * 1e3 / K
+            n_total = int(Uh.shape[0])
+        eng.delete()
+    errs = [float(np.max(np.linalg.norm(a - b, axis=0) / np.linalg.norm(b, axis=0)))
+            for a, b in zip(sols["mixed"], sols["fp64"])]
+    # the plain FP64 single-solve engine: each problem alone, one right-hand side per launch
+    single_ms = 0.0
+    for P in probs:
+        P1 = workloads.make_problem(P.name, P.A, P.U[:, :1], P.Q, P.lam, P.funcs[:1], P.m, P.C, P.l1, P.lN,
+                                    degree=P.d)
+        e = Engine.from_problem(P1, precision="fp64", sync=False)
+        single_ms += P.R * _timed_solves(e, stream, max(2, K // 2), 1)
+        e.delete()
+    single = nsolves * 1e3 / single_ms
+    # fractional monodomain time loop, CUDA graph of 200 steps
+    Pm, dt, ode, fhn = workloads.monodomain_problem(512)
+    mono = {}
+    Us = {}
+    for prec in ("mixed", "fp64"):
+        e = LanczosEngine(Pm.U, Pm.A, Pm.Q, Pm.lam, Pm.m, Pm.gamma, Pm.gs_re, Pm.gs_im, Pm.flam[:, 0],
+                          Pm.flam[:, 1], dt, ode, fhn["aode"], fhn["bode"], fhn["code"], fhn["vrest"],
+                          fhn["vamp"], fhn["vth"], fhn["vpeak"], fhn["c1ion"], fhn["c2ion"], np.ones(Pm.n),
+                          Pm.wts[0], Pm.wts[1], Pm.shifts, precision=prec, sync=False)
+        e.set_stream(stream.cuda_stream)
+        e.time_loop(200, monodomain=True, graph=True)   # capture + first replay
+        Us[prec] = e.get_U()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        e.time_loop(200, monodomain=True, graph=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        mono[prec] = {"steps_per_s": 200e3 / e0.elapsed_time(e1), "ms_per_step": e0.elapsed_time(e1) / 200}
+        e.delete()
+    mono_err = float(np.linalg.norm(Us["mixed"][:, 0] - Us["fp64"][:, 0]) / np.linalg.norm(Us["fp64"][:, 0]))
+    sizes = [int(P.meta["N"]) for P in probs]
+    line = {"metric": "batched f(A)b solves/s (64 uneven fractional-diffusion problems x 4 RHS, one launch)",
+            "value": res["mixed"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": K, "warmup": W,
+            "ms_per_step": res["mixed"]["ms_per_launch"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32-storage/f64-recurrence",
+            "data": "synthetic (seeded grid sizes and right-hand sides)",
+            "config": {"workload": "batch-64", "problems": len(probs), "nrhs": probs[0].R, "grid_N": [min(sizes), max(sizes)],
+                       "rows_total": int(sum(P.n for P in probs)), "m": probs[0].m, "C": probs[0].C,
+                       "f": "exp(-dt K_alpha lambda^0.75), dt 0.05, K_alpha 1e-4, side 2.5"},
+            "e2e": {"value": nsolves * 1e3 / e2e_ms, "unit": "solves/s", "h2d_bytes_per_step": 8 * n_total * probs[0].R,
+                    "d2h_bytes_per_step": 8 * n_total * probs[0].R},
+            "mixed_batched": res["mixed"], "fp64_batched": res["fp64"],
+            "fp64_single_solve": {"solves_per_s": single, "note": "each problem alone, 1 RHS per launch"},
+            "mixed_batched_over_fp64_single": res["mixed"]["solves_per_s"] / single,
+            "mixed_vs_fp64_rel_err": {"worst": max(errs), "median": float(np.median(errs))},
+            "monodomain_512": {**{f"{p}_steps_per_s": mono[p]["steps_per_s"] for p in mono},
+                               "steps": 200, "graph": True, "m": Pm.m, "C": Pm.C, "k": Pm.k,
+                               "mixed_vs_fp64_after_400_steps": mono_err},
+            "setup_s": setup_s}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
+    if args.workload == "batch-64":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "batched serving is not a reference workload"}))
+        else:
+            run_batch(args)
+        return
+    if args.workload.startswith("fe-adjoint-"):
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the reference has no adjoint"}))
+        else:
+            run_adjoint(args)
+        return
     rank, world, local = dist_env()
     if world > 1 and args.impl == "ours":
         import torch

@@ -137,7 +137,7 @@ class FracFEOperator:
         n = self.st.n
         self.engine = Engine(A0, np.zeros((n, 2)), None, None, None, m, self.gamma, gs.real, gs.imag, [w, w],
                              params.shifts_vector(sigma, m, 2), col_scale=np.ones(2), precision=precision,
-                             sync=False, keep_entry_map=True, **engine_kw)
+                             sync=False, keep_entry_map=True, row_weight=self.st.msqrt, **engine_kw)
         st = self.st
         self.engine.fe_attach(st.ntri, st.ent_ptr, st.ent_tri, st.ent_coef, st.tri_nodes, st.tri_kc)
         self.n, self.ntri = n, st.ntri
@@ -153,31 +153,27 @@ class FracFEOperator:
             self.engine.set_stream(s)
             self._stream = s
 
-    def _solve(self, kappa, u0, u1):
-        """Assemble A(kappa), solve for U = [u0, u1]; returns the solution (2, n)."""
+    def forward(self, kappa, b):
+        """f(A(kappa)) b (CUDA float64 tensors) through gm_fe_forward."""
         import torch
         self._on_current_stream()
         kappa = kappa.detach().to(torch.float64).contiguous()
-        U = torch.stack([u0.detach().to(torch.float64), u1.detach().to(torch.float64)]).contiguous()
-        self.engine.fe_assemble(kappa.data_ptr())
-        self.engine.set_U_device(U.data_ptr())
-        self.engine.solve()
-        X = torch.empty_like(U)
-        self.engine.get_solution_device(X.data_ptr())
-        return X
-
-    def forward(self, kappa, b):
-        """f(A(kappa)) b (CUDA float64 tensors)."""
-        import torch
-        return self._solve(kappa, b, torch.zeros_like(b))[0]
+        b = b.detach().to(torch.float64).contiguous()
+        x = torch.empty_like(b)
+        self.engine.fe_forward(kappa.data_ptr(), b.data_ptr(), x.data_ptr())
+        return x
 
     def backward(self, kappa, b, gx):
-        """(dL/dkappa, dL/db) for dL/dx = gx."""
+        """(dL/dkappa, dL/db) for dL/dx = gx through gm_fe_backward."""
         import torch
-        X = self._solve(kappa, b, gx)
-        dk = torch.empty(self.ntri, dtype=torch.float64, device=X.device)
-        self.engine.fe_gradient(dk.data_ptr())
-        return dk, X[1]
+        self._on_current_stream()
+        kappa = kappa.detach().to(torch.float64).contiguous()
+        b = b.detach().to(torch.float64).contiguous()
+        gx = gx.detach().to(torch.float64).contiguous()
+        dk = torch.empty(self.ntri, dtype=torch.float64, device=b.device)
+        db = torch.empty_like(b)
+        self.engine.fe_backward(kappa.data_ptr(), b.data_ptr(), gx.data_ptr(), dk.data_ptr(), db.data_ptr())
+        return dk, db
 
     def delete(self):
         self.engine.delete()

@@ -64,6 +64,10 @@ struct gm_engine {
   bool l2_window = false;        // launches carry an L2 persisting window over the matrix
   cudaAccessPolicyWindow window = {};
   bool keep_map = false;
+  std::vector<double> roww;      // mixed engine: weights of the diagonal compensation (empty = ones)
+  bool comp = false;             // mixed engine: diagonal compensation on
+  int* row2slot = nullptr;       // device, kept with the entry map: row -> 32 * slice + lane
+  double* d_roww = nullptr;      // device weights (kept with the entry map, mixed)
   // finite-element structure for gm_fe_assemble / gm_fe_gradient
   long long fe_ntri = 0;
   long long* fe_ent_ptr = nullptr;
@@ -72,6 +76,8 @@ struct gm_engine {
   long long* fe_nodes = nullptr;
   double* fe_kc = nullptr;
   double2* fe_buf[6] = {};
+  double* fe_kappa = nullptr;    // kappa copied in by gm_fe_forward / gm_fe_backward
+  double* fe_dk = nullptr;       // dL/dkappa before it is copied out
   long long* csr_ptr = nullptr;  // device CSR row pointer (kept with csr2sell)
   double2* fe_yb = nullptr;
   double2* fe_yg = nullptr;
@@ -272,6 +278,41 @@ int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp, const std:
   long long* d_off;
   int rc;
   if ((rc = dupload(e, &d_off, off.data(), off.size()))) return rc;
+  // Diagonal compensation of the FP32-stored matrix: row r gets the extra
+  // diagonal term c_r = sum_t (a_t 2^-e - fl32(a_t 2^-e)) w_col(t) / w_r, so
+  // that the stored operator maps w exactly as A does.  The small eigenvalues
+  // of a Laplacian-like operator come from cancellation in A w-like products;
+  // rounding every entry independently breaks it (an error of order
+  // eps_32 * a_ii per row, relative to lambda_min), the compensation keeps it.
+  e->kp.dlo = nullptr;
+  if (sizeof(VT) == 4 && e->comp) {
+    std::vector<float> dlo(nsl * 32, 0.f);
+    const bool ones = e->roww.empty();
+    std::vector<int> r2s;
+    if (e->keep_map) r2s.assign(A.ptr.size() - 1, 0);
+    for (long long s = 0; s < nsl; ++s)
+      for (int l = 0; l < 32; ++l) {
+        const long long r = rows[s * 32 + l];
+        if (r < 0) continue;
+        if (e->keep_map) r2s[r] = (int)(s * 32 + l);
+        double corr = 0.0;
+        for (long long t = A.ptr[r]; t < A.ptr[r + 1]; ++t) {
+          const double exact = std::ldexp(A.val[t], -scale_exp);
+          const double err = exact - (double)(float)exact;
+          corr += ones ? err : err * e->roww[A.col[t]];
+        }
+        dlo[s * 32 + l] = (float)(ones ? corr : corr / e->roww[r]);
+      }
+    float* d_dlo;
+    if ((rc = dupload(e, &d_dlo, dlo.data(), dlo.size()))) return rc;
+    e->kp.dlo = d_dlo;
+    if (e->keep_map) {
+      if ((rc = dupload(e, &e->row2slot, r2s.data(), r2s.size()))) return rc;
+      std::vector<double> w = e->roww;
+      if (w.empty()) w.assign(A.ptr.size() - 1, 1.0);
+      if ((rc = dupload(e, &e->d_roww, w.data(), w.size()))) return rc;
+    }
+  }
   // values and column indices in one allocation, so that one L2 access-policy
   // window can cover the whole matrix
   const size_t vbytes = ((size_t)padded * sizeof(VT) + 255) & ~(size_t)255;
@@ -537,6 +578,8 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
     return fail(e, GM_ERR_ARG, "lanczos_create:invalidNumInputs: struct_version %d != %d", a->struct_version, GM_CREATE_ARGS_VERSION);
   const int np = (int)probs.size();
   if (np < 1) return fail(e, GM_ERR_ARG, "batch_create: no problems");
+  if (a->gamma_size < 1 || a->gamma_size > GM_MAX_DEG + 1)
+    return fail(e, GM_ERR_ARG, "lanczos_create:bad_gamma: polynomial degree must be 0..%d (gamma_size %d)", GM_MAX_DEG, a->gamma_size);
   if (a->nrhs != 1 && a->nrhs != 2 && a->nrhs != 4) return fail(e, GM_ERR_ARG, "lanczos_create:badU: nrhs must be 1, 2 or 4 (got %d)", a->nrhs);
   if (a->num_eigs < 0 || (a->num_eigs > 0 && (!a->Q || !a->flam)))
     return fail(e, GM_ERR_ARG, "lanczos_create:badQ: num_eigs %d needs Q and f(lambda)", a->num_eigs);
@@ -561,6 +604,13 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
   if (ntot > 2147483647LL) return fail(e, GM_ERR_UNSUPPORTED, "n above 2^31-1");
 
   e->keep_map = a->keep_entry_map != 0 && np == 1;
+  e->comp = a->precision == GM_MIXED && a->diag_compensation == 0;
+  if (e->comp && a->row_weight) {
+    if (np != 1) return fail(e, GM_ERR_ARG, "row_weight applies to a single problem");
+    e->roww.assign(a->row_weight, a->row_weight + probs[0].n);
+    for (double w : e->roww)
+      if (!(w > 0.0) || !std::isfinite(w)) return fail(e, GM_ERR_ARG, "row_weight entries must be positive and finite");
+  }
   if (a->keep_entry_map && probs[0].format != GM_CSR) return fail(e, GM_ERR_ARG, "keep_entry_map needs a CSR matrix");
   e->n = ntot; e->nprob = np; e->R = a->nrhs; e->m = a->subspace_size; e->d = a->gamma_size - 1;
   e->C = a->contour_size; e->k = a->num_eigs; e->prec = a->precision; e->sync_mode = a->sync_mode;
@@ -1027,6 +1077,8 @@ int gm_fe_attach(gm_handle h, int64_t ntri, const int64_t* ent_ptr, const int32_
   if ((rc = dupload(h, &h->fe_ent_coef, ent_coef, nc))) return rc;
   if ((rc = dupload(h, &h->fe_nodes, reinterpret_cast<const long long*>(tri_nodes), 3 * ntri))) return rc;
   if ((rc = dupload(h, &h->fe_kc, tri_kc, 9 * ntri))) return rc;
+  if ((rc = dalloc(h, &h->fe_kappa, (size_t)ntri))) return rc;
+  if ((rc = dalloc(h, &h->fe_dk, (size_t)ntri))) return rc;
   return GM_OK;
 }
 
@@ -1038,6 +1090,10 @@ int gm_fe_assemble(gm_handle h, const double* kappa_dev) {
   if (h->prec == GM_FP64)
     gm::k_fe_assemble<double><<<blocks, 256, 0, h->stream>>>(nnz, h->fe_ent_ptr, h->fe_ent_tri, h->fe_ent_coef, kappa_dev,
                                                              h->csr2sell, (double*)h->kp.val, h->scale_exp);
+  else if (h->comp)
+    gm::k_fe_assemble_rows<<<(unsigned)((h->n + 255) / 256), 256, 0, h->stream>>>(
+        h->n, h->csr_ptr, h->kp.col, h->fe_ent_ptr, h->fe_ent_tri, h->fe_ent_coef, kappa_dev, h->csr2sell,
+        (float*)h->kp.val, h->scale_exp, h->d_roww, h->row2slot, const_cast<float*>(h->kp.dlo));
   else
     gm::k_fe_assemble<float><<<blocks, 256, 0, h->stream>>>(nnz, h->fe_ent_ptr, h->fe_ent_tri, h->fe_ent_coef, kappa_dev,
                                                             h->csr2sell, (float*)h->kp.val, h->scale_exp);
@@ -1120,6 +1176,69 @@ int gm_fe_gradient(gm_handle h, double* dkappa_dev) {
   GM_CUDA(h, cudaGetLastError());
   h->launches++;
   return h->sync_mode ? check_sync(h) : GM_OK;
+}
+
+// host (pageable or pinned) or device pointer: cudaMemcpyDefault resolves it
+static bool host_memory(const void* p) {
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return true;
+  }
+  return at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged;
+}
+
+// U = [b, g] (g = 0 when null) from host or device memory, via the stage buffer
+static int fe_load(gm_handle h, const double* kappa, const double* b, const double* g) {
+  if (!h->fe_kappa) return fail(h, GM_ERR_STATE, "fe_forward/fe_backward before fe_attach");
+  if (h->R != 2) return fail(h, GM_ERR_UNSUPPORTED, "fe_forward/fe_backward need nrhs = 2");
+  if (!kappa || !b) return fail(h, GM_ERR_ARG, "fe_forward/fe_backward: null kappa or b");
+  const size_t nb = (size_t)h->n * sizeof(double);
+  GM_CUDA(h, cudaMemcpyAsync(h->fe_kappa, kappa, (size_t)h->fe_ntri * sizeof(double), cudaMemcpyDefault, h->stream));
+  int rc = gm_fe_assemble(h, h->fe_kappa);
+  if (rc) return rc;
+  GM_CUDA(h, cudaMemcpyAsync(h->stage, b, nb, cudaMemcpyDefault, h->stream));
+  if (g)
+    GM_CUDA(h, cudaMemcpyAsync(h->stage + h->n, g, nb, cudaMemcpyDefault, h->stream));
+  else
+    GM_CUDA(h, cudaMemsetAsync(h->stage + h->n, 0, nb, h->stream));
+  if ((rc = set_U_common(h, h->stage, true))) return rc;
+  return gm_solve(h);
+}
+
+// column c of the solution (interleaved [n][2]) to dst (host or device)
+static int fe_store_col(gm_handle h, int c, double* dst) {
+  const long long total = h->n * h->R;
+  k_pack_out<<<(unsigned)((total + 255) / 256), 256, 0, h->stream>>>(h->kp.S, h->stage, h->n, h->R);
+  GM_CUDA(h, cudaGetLastError());
+  h->launches++;
+  GM_CUDA(h, cudaMemcpyAsync(dst, h->stage + (size_t)c * h->n, (size_t)h->n * sizeof(double), cudaMemcpyDefault,
+                             h->stream));
+  return GM_OK;
+}
+
+int gm_fe_forward(gm_handle h, const double* kappa, const double* b, double* x) {
+  if (!h) return GM_ERR_ARG;
+  if (!x) return fail(h, GM_ERR_ARG, "fe_forward: null x");
+  int rc = fe_load(h, kappa, b, nullptr);
+  if (!rc) rc = fe_store_col(h, 0, x);
+  if (rc) return rc;
+  return (h->sync_mode || host_memory(x)) ? check_sync(h) : GM_OK;
+}
+
+int gm_fe_backward(gm_handle h, const double* kappa, const double* b, const double* g, double* dkappa, double* db) {
+  if (!h) return GM_ERR_ARG;
+  if (!g || !dkappa) return fail(h, GM_ERR_ARG, "fe_backward: null g or dkappa");
+  int rc = fe_load(h, kappa, b, g);
+  if (rc) return rc;
+  const int saved = h->sync_mode;
+  h->sync_mode = 0;
+  rc = gm_fe_gradient(h, h->fe_dk);
+  h->sync_mode = saved;
+  if (rc) return rc;
+  GM_CUDA(h, cudaMemcpyAsync(dkappa, h->fe_dk, (size_t)h->fe_ntri * sizeof(double), cudaMemcpyDefault, h->stream));
+  if (db && (rc = fe_store_col(h, 1, db))) return rc;
+  return (h->sync_mode || host_memory(dkappa) || (db && host_memory(db))) ? check_sync(h) : GM_OK;
 }
 
 int gm_time_loop(gm_handle h, int nsteps, int mode, int use_graph) {

@@ -39,6 +39,7 @@ struct KParams {
   const int* col;
   const void* val;
   const int* perm;
+  const float* dlo;     // mixed: per-slot-row diagonal compensation (slot order), or null
   const double* gamma;
   const double* gs_re;
   const double* gs_im;
@@ -217,6 +218,19 @@ __device__ __forceinline__ void spmv_slot(const KParams& kp, long long s, int la
         for (int r = 0; r < R; ++r) acc[r] = Pol::acc(acc[r], aa[u], xv[u][r]);
       }
   }
+  if constexpr (Pol::kMixed) {
+    // diagonal compensation of the FP32-stored values (c_r x_r)
+    if (kp.dlo) {
+      const long long row = slot_row(kp, s, lane);
+      if (row >= 0) {
+        const float dl = kp.dlo[s * 32 + lane];
+        XT xr[R];
+        VecIO<R>::ld(x + row * R, xr);
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[r] = Pol::acc(acc[r], dl, xr[r]);
+      }
+    }
+  }
 }
 
 template <class Pol> __device__ __forceinline__ typename Pol::AT h_load_at(const typename Pol::HT& h);
@@ -335,11 +349,15 @@ __device__ __forceinline__ void spmv_pass(const KParams& kp, const Ctx& c, ColSt
 // Block-uniform Lanczos scalars live in shared memory, not registers: with R
 // right-hand sides they would otherwise occupy ~10R registers across every
 // SpMV pass and push the passes into local-memory spills.
+#ifndef GM_MAX_DEG
+#define GM_MAX_DEG 32
+#endif
 template <class Pol, int R>
 struct LanczosScalars {
-  double beta[R], rbeta[R], alpha[R], tot[R];
+  double beta[R], rbeta[R], rbp[R], alpha[R], tot[R];
   int broken[R];
   typename Pol::ST sc[R], rb[R], bj[R], al[R];
+  typename Pol::ST gr[GM_MAX_DEG + 1][R];   // gamma_h rbeta_j of the current step
   int all_broken;
 };
 
@@ -402,6 +420,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
       sh.beta[r] = sqrt(sh.tot[r]);
       sh.broken[r] = !(sh.beta[r] > 0.0);
       sh.rbeta[r] = sh.broken[r] ? 0.0 : 1.0 / sh.beta[r];
+      sh.rbp[r] = 0.0;
       if (g.bl == 0) {
         aab[(long long)(m + 1) * (R + r)] = sh.beta[r];
         meff[r] = sh.broken[r] ? 0 : m;
@@ -410,16 +429,28 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
     }
   }
   __syncthreads();
+  // Inside the recurrence the Lanczos vector is v_j = rbeta_j w_j, formed
+  // from the stored work vector w_j (src) in the accumulator precision in
+  // every pass, so the polynomial's terms all act on the same vector: its
+  // monomial terms cancel strongly, and mixing w_j-based and separately
+  // rounded v_j terms would turn the storage rounding into an error of
+  // p(B) v_j.  The rounded v_j is stored in V for the apply only.  v_{j-1}
+  // is rbeta_{j-1} w_{j-1}, read from the work buffer this step overwrites.
   const BT* src = W1;
   for (int j = 0; j < m; ++j) {
     BT* Vj = V + (long long)j * n * R;
-    const BT* Vjm1 = j > 0 ? V + (long long)(j - 1) * n * R : V;
     BT* Wout = (j & 1) ? W1 : W0;
+    // w = B v_j - beta_j v_{j-1} goes to the Horner buffer the last pass does
+    // not read, in the accumulator precision; pass B subtracts alpha_j v_j and
+    // rounds once to storage (rounding before the subtraction would make the
+    // storage error relative to |w| instead of to beta_{j+1} << |w|).
+    HT* const Hw = (d & 1) ? H0 : H1;
     if (c.tid == 0) {
       for (int r = 0; r < R; ++r) {
         sh.sc[r] = Pol::scalar(sh.rbeta[r] * gam[0]);
         sh.rb[r] = Pol::scalar(sh.rbeta[r]);
-        sh.bj[r] = Pol::scalar(sh.beta[r]);
+        sh.bj[r] = Pol::scalar(sh.beta[r] * sh.rbp[r]);
+        for (int h = 1; h <= d; ++h) sh.gr[h][r] = Pol::scalar(gam[h] * sh.rbeta[r]);
       }
     }
     __syncthreads();
@@ -439,20 +470,19 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
 #pragma unroll
         for (int r = 0; r < R; ++r) w[r] = Pol::mul(z[r], sh.sc[r]);
         if (j > 0) {
-          BT vp[R];
-          VecIO<R>::ld(Vjm1 + row * R, vp);
+          BT wp[R];
+          VecIO<R>::ld(Wout + row * R, wp);   // w_{j-1}
 #pragma unroll
-          for (int r = 0; r < R; ++r) w[r] = Pol::sub_mul(w[r], sh.bj[r], vp[r]);
+          for (int r = 0; r < R; ++r) w[r] = Pol::sub_mul(w[r], sh.bj[r], wp[r]);
         }
-        BT wb[R];
+        HT wh[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) { wb[r] = Pol::to_b(w[r]); apa[r] = Pol::dot(apa[r], w[r], v[r]); }
-        VecIO<R>::st(Wout + row * R, wb);
+        for (int r = 0; r < R; ++r) { wh[r] = Pol::to_h(w[r]); apa[r] = Pol::dot(apa[r], w[r], sv[r]); }
+        VecIO<R>::st(Hw + row * R, wh);
       });
     } else {
       // Horner pass 1: u = gamma_1 v_j + A (gamma_0 v_j); stores v_j
       {
-        const typename Pol::ST g1 = Pol::scalar(gam[1]);
         spmv_pass<Pol, R, BT>(kp, c, cs, src, [&](long long s, AT (&z)[R]) {
           const long long row = slot_row(kp, s, c.lane);
           if (row < 0) return;
@@ -463,24 +493,23 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
           VecIO<R>::st(Vj + row * R, v);
           HT u[R];
 #pragma unroll
-          for (int r = 0; r < R; ++r) u[r] = Pol::to_h(Pol::add_mul(Pol::mul(z[r], sh.sc[r]), g1, v[r]));
+          for (int r = 0; r < R; ++r) u[r] = Pol::to_h(Pol::add_mul(Pol::mul(z[r], sh.sc[r]), sh.gr[1][r], sv[r]));
           VecIO<R>::st(H1 + row * R, u);
         });
       }
       ps.done();
       if (!ps.before_next()) return false;
       for (int h = 2; h <= d; ++h) {
-        const typename Pol::ST gh = Pol::scalar(gam[h]);
         const HT* hin = (h & 1) ? H0 : H1;
         HT* hout = (h & 1) ? H1 : H0;
         spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
           const long long row = slot_row(kp, s, c.lane);
           if (row < 0) return;
-          BT v[R];
-          VecIO<R>::ld(Vj + row * R, v);
+          BT sv[R];
+          VecIO<R>::ld(src + row * R, sv);
           HT u[R];
 #pragma unroll
-          for (int r = 0; r < R; ++r) u[r] = Pol::to_h(Pol::add_mul(z[r], gh, v[r]));
+          for (int r = 0; r < R; ++r) u[r] = Pol::to_h(Pol::add_mul(z[r], sh.gr[h][r], sv[r]));
           VecIO<R>::st(hout + row * R, u);
         });
         ps.done();
@@ -491,21 +520,21 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
       spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
         const long long row = slot_row(kp, s, c.lane);
         if (row < 0) return;
-        BT v[R];
-        VecIO<R>::ld(Vj + row * R, v);
+        BT sv[R];
+        VecIO<R>::ld(src + row * R, sv);
         AT w[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) w[r] = z[r];
         if (j > 0) {
-          BT vp[R];
-          VecIO<R>::ld(Vjm1 + row * R, vp);
+          BT wp[R];
+          VecIO<R>::ld(Wout + row * R, wp);   // w_{j-1}
 #pragma unroll
-          for (int r = 0; r < R; ++r) w[r] = Pol::sub_mul(w[r], sh.bj[r], vp[r]);
+          for (int r = 0; r < R; ++r) w[r] = Pol::sub_mul(w[r], sh.bj[r], wp[r]);
         }
-        BT wb[R];
+        HT wh[R];
 #pragma unroll
-        for (int r = 0; r < R; ++r) { wb[r] = Pol::to_b(w[r]); apa[r] = Pol::dot(apa[r], w[r], v[r]); }
-        VecIO<R>::st(Wout + row * R, wb);
+        for (int r = 0; r < R; ++r) { wh[r] = Pol::to_h(w[r]); apa[r] = Pol::dot(apa[r], w[r], sv[r]); }
+        VecIO<R>::st(Hw + row * R, wh);
       });
     }
     {
@@ -518,7 +547,11 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
     if (!bar.sync()) return false;
     grid_total_smem<R>(part_a + g.gb, G, g.Gp, sh.alpha);
     if (c.tid == 0) {
-      for (int r = 0; r < R; ++r) sh.al[r] = Pol::scalar(sh.alpha[r]);
+      // alpha_j = w^T v_j = rbeta_j (w^T w_j); pass B subtracts alpha_j rbeta_j w_j
+      for (int r = 0; r < R; ++r) {
+        sh.alpha[r] *= sh.rbeta[r];
+        sh.al[r] = Pol::scalar(sh.alpha[r] * sh.rbeta[r]);
+      }
     }
     __syncthreads();
     // pass B: w -= alpha_j v_j; beta_{j+1} = ||w||
@@ -527,12 +560,13 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
 #pragma unroll
       for (int r = 0; r < R; ++r) bpa[r] = Pol::zero();
       for (long long i = g.gt; i < g.r1; i += g.tt) {
+        HT wh[R];
         BT wb[R], v[R];
-        VecIO<R>::ld(Wout + i * R, wb);
-        VecIO<R>::ld(Vj + i * R, v);
+        VecIO<R>::ld(Hw + i * R, wh);
+        VecIO<R>::ld(src + i * R, v);   // w_j
 #pragma unroll
         for (int r = 0; r < R; ++r) {
-          AT w = Pol::sub_mul(Pol::from_b(wb[r]), sh.al[r], v[r]);
+          AT w = Pol::sub_mul(h_load_at<Pol>(wh[r]), sh.al[r], v[r]);
           wb[r] = Pol::to_b(w);
           bpa[r] = Pol::dot_self(bpa[r], w);
         }
@@ -560,6 +594,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
           sh.broken[r] = 1;
           if (g.bl == 0) meff[r] = j + 1;
         }
+        sh.rbp[r] = sh.rbeta[r];
         sh.beta[r] = sh.broken[r] ? 0.0 : bn;
         sh.rbeta[r] = sh.broken[r] ? 0.0 : 1.0 / bn;
         all = all && sh.broken[r];

@@ -37,6 +37,31 @@ __global__ void k_fe_assemble(long long nnz, const long long* __restrict__ ent_p
   val[slot[t]] = (VT)ldexp(acc, -se);
 }
 
+// Mixed engine: values of one row of A(kappa) in FP32 (stored as A 2^-se) and
+// the row's diagonal compensation c_r = sum_t (a_t - fl32(a_t)) w_col / w_r,
+// the same correction the engine computes at create (one thread per row,
+// fixed order).
+__global__ void k_fe_assemble_rows(long long n, const long long* __restrict__ ptr, const int* __restrict__ col,
+                                   const long long* __restrict__ ent_ptr, const int* __restrict__ ent_tri,
+                                   const double* __restrict__ ent_coef, const double* __restrict__ kappa,
+                                   const int* __restrict__ slot, float* __restrict__ val, int se,
+                                   const double* __restrict__ w, const int* __restrict__ row2slot,
+                                   float* __restrict__ dlo) {
+  const long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  double corr = 0.0;
+  for (long long t = ptr[r]; t < ptr[r + 1]; ++t) {
+    double acc = 0.0;
+    for (long long p = ent_ptr[t]; p < ent_ptr[t + 1]; ++p) acc = fma(kappa[ent_tri[p]], ent_coef[p], acc);
+    const double exact = ldexp(acc, -se);
+    const int st = slot[t];
+    const float v = (float)exact;
+    val[st] = v;
+    corr += (exact - (double)v) * w[col[st]];
+  }
+  dlo[row2slot[r]] = (float)(corr / w[r]);
+}
+
 // Zb[i][j] = sum_q V[q][i][0] yb'[j][q], Zg[i][j] = sum_q V[q][i][1] yg[j][q]
 // (complex; yb' = y_b / w); rows by thread, shifts in chunks of JC whose
 // coefficients sit in shared memory.

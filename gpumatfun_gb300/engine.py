@@ -34,7 +34,7 @@ EXPORTED_SYMBOLS = [
     "gm_get_solution", "gm_solve", "gm_solve_host", "gm_sync", "gm_set_stream",
     "gm_phase_times", "gm_info", "gm_get_meff", "gm_last_error", "gm_version",
     "gm_lin_sys_solves_noalloc", "gm_batch_create", "gm_time_loop", "gm_fe_attach", "gm_fe_assemble",
-    "gm_fe_gradient", "gm_get_solution_device",
+    "gm_fe_gradient", "gm_get_solution_device", "gm_fe_forward", "gm_fe_backward",
 ]
 
 _dp = ct.POINTER(ct.c_double)
@@ -61,6 +61,7 @@ class CreateArgs(ct.Structure):
         ("barrier_timeout_s", ct.c_double), ("breakdown_tol", ct.c_double),
         ("sync_policy", ct.c_int), ("col_staging", ct.c_int), ("keep_entry_map", ct.c_int),
         ("l2_window", ct.c_int),
+        ("row_weight", _dp), ("diag_compensation", ct.c_int),
     ]
 
 
@@ -109,6 +110,8 @@ def load_library(build_if_missing: bool = False) -> ct.CDLL:
     lib.gm_fe_assemble.argtypes = [h, ct.c_void_p]
     lib.gm_fe_gradient.argtypes = [h, ct.c_void_p]
     lib.gm_get_solution_device.argtypes = [h, ct.c_void_p]
+    lib.gm_fe_forward.argtypes = [h, ct.c_void_p, ct.c_void_p, ct.c_void_p]
+    lib.gm_fe_backward.argtypes = [h, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]
     lib.gm_phase_times.argtypes = [h, ct.POINTER(ct.c_float)]
     lib.gm_info.argtypes = [h, _lp]
     lib.gm_get_meff.argtypes = [h, ct.POINTER(ct.c_int)]
@@ -144,7 +147,8 @@ class Engine:
                  precision: str | int = "fp64", sync: bool = True, threads: int = 0,
                  blocks_per_sm: int = 0, sell_sigma: int = 0, timeout_s: float = 0.0,
                  breakdown_tol: float = 0.0, matrix_format: str = "csr", sync_policy: int = 0,
-                 col_staging: int = 0, keep_entry_map: bool = False, l2_window: int = 0):
+                 col_staging: int = 0, keep_entry_map: bool = False, l2_window: int = 0,
+                 row_weight=None, diag_compensation: int = 0):
         self._lib = load_library()
         self._h = ct.c_void_p()
         n = A.shape[0]
@@ -200,7 +204,10 @@ class Engine:
         a.col_staging = int(col_staging)
         a.keep_entry_map = 1 if keep_entry_map else 0
         a.l2_window = int(l2_window)
-        self._keep = (ptr, ind, val, U, Q, lam, flam, gamma, gs_re, gs_im, wts, shifts, cs, mass, ode)
+        rw = _f64(row_weight) if row_weight is not None else None
+        a.row_weight = _ptr(rw) if rw is not None else None
+        a.diag_compensation = int(diag_compensation)
+        self._keep = (ptr, ind, val, U, Q, lam, flam, gamma, gs_re, gs_im, wts, shifts, cs, mass, ode, rw)
         rc = self._lib.gm_lanczos_create(ct.byref(a), ct.byref(self._h))
         self._keep = None
         if rc != 0:
@@ -300,6 +307,15 @@ class Engine:
         """dL/dkappa (device pointer, ntri doubles) after solving for U = [b, g]."""
         self._check(self._lib.gm_fe_gradient(self._h, ct.c_void_p(dkappa_ptr)))
 
+    def fe_forward(self, kappa: int, b: int, x: int):
+        """x = f(A(kappa)) b; arguments are pointers (host or device)."""
+        self._check(self._lib.gm_fe_forward(self._h, ct.c_void_p(kappa), ct.c_void_p(b), ct.c_void_p(x)))
+
+    def fe_backward(self, kappa: int, b: int, g: int, dkappa: int, db: int | None):
+        """dL/dkappa and dL/db for dL/dx = g; arguments are pointers (host or device)."""
+        self._check(self._lib.gm_fe_backward(self._h, ct.c_void_p(kappa), ct.c_void_p(b), ct.c_void_p(g),
+                                             ct.c_void_p(dkappa), ct.c_void_p(db or 0)))
+
     def get_update(self) -> np.ndarray:
         return self._out(self._lib.gm_get_update)
 
@@ -373,6 +389,7 @@ class Engine:
     @classmethod
     def from_problem(cls, P, **kw) -> "Engine":
         """Engine for a ``workloads.FabProblem``."""
+        kw.setdefault("row_weight", getattr(P, "row_weight", None))
         return cls(P.A, P.U, P.Q, P.lam, P.flam, P.m, P.gamma, P.gs_re, P.gs_im, P.wts, P.shifts,
                    col_scale=P.col_scale if P.col_scale is not None else np.ones(P.R), **kw)
 
@@ -406,7 +423,7 @@ class BatchEngine(Engine):
 
     def __init__(self, problems: Sequence, precision: str | int = "fp64", sync: bool = True,
                  threads: int = 0, blocks_per_sm: int = 0, sell_sigma: int = 0, timeout_s: float = 0.0,
-                 sync_policy: int = 0, col_staging: int = 0):
+                 sync_policy: int = 0, col_staging: int = 0, diag_compensation: int = 0):
         self._lib = load_library()
         self._h = ct.c_void_p()
         P0 = problems[0]
@@ -439,6 +456,7 @@ class BatchEngine(Engine):
         a.sync_mode = 1 if sync else 0
         a.threads_per_block, a.blocks_per_sm, a.sell_sigma = threads, blocks_per_sm, sell_sigma
         a.barrier_timeout_s, a.sync_policy, a.col_staging = timeout_s, int(sync_policy), int(col_staging)
+        a.diag_compensation = int(diag_compensation)
         rc = self._lib.gm_batch_create(len(problems), arr, ct.byref(a), ct.byref(self._h))
         del keep
         if rc != 0:

@@ -44,6 +44,7 @@ class FabProblem:
     lN: float
     col_scale: np.ndarray | None = None
     meta: dict = field(default_factory=dict)
+    row_weight: np.ndarray | None = None   # near-null vector of A (mixed engine's diagonal compensation)
 
     @property
     def n(self):
@@ -67,7 +68,7 @@ class FabProblem:
 
 
 def make_problem(name, A, U, Q, lam, funcs: Sequence[Callable], m, C, l1, lN,
-                 degree=0, prob_dim=2.0, col_scale=None, meta=None) -> FabProblem:
+                 degree=0, prob_dim=2.0, col_scale=None, meta=None, row_weight=None) -> FabProblem:
     """Assemble the method parameters for operator A (startup_nicksmethod_GPU.m:159-218)."""
     A = sp.csr_matrix(A)
     A.sort_indices()
@@ -85,7 +86,7 @@ def make_problem(name, A, U, Q, lam, funcs: Sequence[Callable], m, C, l1, lN,
                       flam=flam, m=int(m), gamma=gamma, gs_re=np.ascontiguousarray(gs.real),
                       gs_im=np.ascontiguousarray(gs.imag), wts=wts, shifts=shifts, sigma=sigma,
                       contour=con, funcs=list(funcs), l1=float(l1), lN=float(lN),
-                      col_scale=col_scale, meta=dict(meta or {}))
+                      col_scale=col_scale, meta=dict(meta or {}), row_weight=row_weight)
 
 
 def fd2d_problem(N: int, k: int, m: int, C: int, funcs, R: int = 1, scale: float = 1.0,
@@ -191,7 +192,8 @@ def fe_disk_problem(n_target: int, k: int, m: int, C: int, degree: int, alpha: f
     U /= np.linalg.norm(U, axis=0, keepdims=True)
     f = params.frac_power(-alpha / 2)
     return make_problem(name, A, U, Q, lam, [f] * R, m, C, l1, lmax, degree=degree,
-                        prob_dim=lmax / 4, meta=dict(n_target=n_target, nt=mesh.tris.shape[0], seed=seed))
+                        prob_dim=lmax / 4, meta=dict(n_target=n_target, nt=mesh.tris.shape[0], seed=seed),
+                        row_weight=ms)
 
 
 def config2(n_target: int = 1_000_000, R: int = 1, seed: int = 0) -> FabProblem:
@@ -219,7 +221,7 @@ def cached_problem(name: str, R: int = 1, cache_dir: str | None = None, seed: in
     n_target = 1_000_000 if tag == "1M" else int(tag)
     cache_dir = cache_dir or os.environ.get("GPUMATFUN_CACHE", os.path.join(os.environ.get("TMPDIR", "/tmp"), "gpumatfun_cache"))
     os.makedirs(cache_dir, exist_ok=True)
-    key = hashlib.sha1(f"fe-disk|{n_target}|k20|seed{seed}|v1".encode()).hexdigest()[:12]
+    key = hashlib.sha1(f"fe-disk|{n_target}|k20|seed{seed}|v2".encode()).hexdigest()[:12]
     path = os.path.join(cache_dir, f"fe-disk-{n_target}-{key}.npz")
     alpha = 1.6
     f = params.frac_power(-alpha / 2)
@@ -233,14 +235,14 @@ def cached_problem(name: str, R: int = 1, cache_dir: str | None = None, seed: in
             U /= np.linalg.norm(U, axis=0, keepdims=True)
         return make_problem(f"fe-disk-{tag}-fp64", A, U[:, :R], z["Q"], z["lam"], [f] * R, 80, 48,
                             float(z["l1"]), float(z["lN"]), degree=8, prob_dim=float(z["lN"]) / 4,
-                            meta=dict(n_target=n_target, seed=seed, cached=True))
+                            meta=dict(n_target=n_target, seed=seed, cached=True), row_weight=z["ms"])
     P = fe_disk_problem(n_target, 20, 80, 48, 8, alpha=alpha, R=max(R, 4), seed=seed, name=f"fe-disk-{tag}-fp64")
     tmp = path + f".tmp{os.getpid()}.npz"
     np.savez(tmp, data=P.A.data, indices=P.A.indices, indptr=P.A.indptr, shape=np.array(P.A.shape),
-             U=P.U, Q=P.Q, lam=P.lam, l1=P.l1, lN=P.lN)
+             U=P.U, Q=P.Q, lam=P.lam, l1=P.l1, lN=P.lN, ms=P.row_weight)
     os.replace(tmp, path)
     return make_problem(P.name, P.A, P.U[:, :R], P.Q, P.lam, [f] * R, 80, 48, P.l1, P.lN, degree=8,
-                        prob_dim=P.lN / 4, meta=P.meta)
+                        prob_dim=P.lN / 4, meta=P.meta, row_weight=P.row_weight)
 
 
 def batch_sizes(nprob: int, lo: int = 64, hi: int = 1024, seed: int = 0) -> np.ndarray:
@@ -250,15 +252,18 @@ def batch_sizes(nprob: int, lo: int = 64, hi: int = 1024, seed: int = 0) -> np.n
 
 
 def config5_batch(nprob: int = 64, R: int = 4, seed: int = 0, lo: int = 64, hi: int = 1024,
-                  m: int = 60, C: int = 32, alpha: float = 1.5, degree: int = 0) -> list:
+                  m: int = 32, C: int = 32, alpha: float = 1.5, degree: int = 0, side: float = 2.5,
+                  Kalpha: float = 1e-4, dt: float = 0.05) -> list:
     """Batched serving-style workload: ``nprob`` independent fractional
-    diffusion problems f(A) b with f = x^(-alpha/2) on 2D 5-point Dirichlet
-    Laplacians (side N drawn log-uniformly in [lo, hi], scaled by (N+1)^2),
-    each with R right-hand sides, all solved by one launch."""
-    f = params.frac_power(-alpha / 2)
+    diffusion problems, each one time step u <- exp(-dt K_alpha A^(alpha/2)) u
+    (the monodomain's physical parameters: square of side 2.5, K_alpha = 1e-4,
+    dt = 0.05, alpha = 1.5) on a 2D 5-point Dirichlet Laplacian with N^2
+    interior nodes (N log-uniform in [lo, hi], A scaled by 1/h^2,
+    h = side/(N+1)), R right-hand sides each, all solved by one launch."""
+    f = params.frac_exp(Kalpha * dt, alpha)
     out = []
     for i, N in enumerate(batch_sizes(nprob, lo, hi, seed)):
-        P = fd2d_problem(int(N), 0, m, C, [f] * R, R=R, scale=(N + 1.0) ** 2, seed=seed + 1 + i,
+        P = fd2d_problem(int(N), 0, m, C, [f] * R, R=R, scale=((N + 1.0) / side) ** 2, seed=seed + 1 + i,
                          degree=degree, name=f"batch{i}-{N}")
         out.append(P)
     return out
@@ -311,3 +316,26 @@ def monodomain_problem(N: int = 512, alpha: float = 1.5, Kalpha: float = 1e-4, d
     P = make_problem(f"monodomain-{N}", A, U, Q, lam, [f1, f2], m, C, l1, lN, degree=0, prob_dim=2.0,
                      meta=dict(N=N, alpha=alpha, Kalpha=Kalpha, dt=dt, eta=eta, k=k))
     return P, dt, ode, dict(p)
+
+
+def adjoint_case(n_target: int = 250_000, seed: int = 0, sigma_g: float = 1.0, ell: float = 0.1):
+    """Inverse-problem workload on the FE disk: the mesh, the current per-triangle
+    coefficient kappa, the ground truth kappa* (two independent Gaussian fields,
+    kappa = exp(g)) and a normalised b ~ U[0,1).  The data d = f(A(kappa*)) b
+    plus 1% noise is synthesised by the caller with the engine it measures."""
+    mesh = problems.disk_mesh(n_target, seed=seed)
+    cent = mesh.nodes[mesh.tris].mean(axis=1)
+    kstar = np.exp(problems.gaussian_random_field(cent, sigma=sigma_g, ell=ell, seed=seed + 1))
+    kappa = np.exp(problems.gaussian_random_field(cent, sigma=sigma_g, ell=ell, seed=seed + 7))
+    n = int((~mesh.boundary).sum())
+    rng = np.random.default_rng(seed + 2)
+    b = rng.random(n)
+    b /= np.linalg.norm(b)
+    return mesh, kappa, kstar, b
+
+
+# Method parameters of the adjoint workload: degree-16 Jacobi polynomial and
+# m = 900 converge f(A)b on the 250k-node disk (condition number ~4e6 for this
+# coefficient field) to ~7e-10 vs m = 1600 (m = 500: 6e-6, m = 700: 8e-8);
+# degree 24 is not usable (its monomial coefficients lose the approximation).
+ADJOINT_PARAMS = dict(alpha=1.6, m=900, C=32, degree=16, margin=1.25)

@@ -115,6 +115,12 @@ typedef struct gm_create_args {
   int l2_window;               /* 0 = launches keep the SELL matrix resident in L2
                                   (persisting access-policy window, up to the
                                   device's persisting limit; default), 1 = off     */
+  const double* row_weight;    /* mixed engine, n entries: the FP32-stored matrix
+                                  gets a per-row diagonal correction so that
+                                  A' w = A w exactly for this w (the operator's
+                                  near-null vector: ones for a graph Laplacian,
+                                  M^{1/2} 1 for M^{-1/2} K M^{-1/2}); NULL = ones  */
+  int diag_compensation;       /* mixed engine: 0 = on (default), 1 = off          */
 } gm_create_args;
 
 /* Fill *args with defaults (zeros, struct_version, sync_mode = 1, nrhs = 2). */
@@ -246,6 +252,18 @@ int gm_fe_assemble(gm_handle h, const double* kappa_dev);
  * shifted solves (q_j the shifted polynomial, gamma_s(:, j)).
  * dL/db = f(A) g is column 1 of the solution. */
 int gm_fe_gradient(gm_handle h, double* dkappa_dev);
+
+/* One forward evaluation x = f(A(kappa)) b: assemble, solve with U = [b, 0],
+ * copy column 0.  kappa (ntri), b and x (n) may be host or device memory
+ * (UVA); results in host memory are complete on return, device results
+ * follow the handle's stream order. */
+int gm_fe_forward(gm_handle h, const double* kappa, const double* b, double* x);
+
+/* The backward entry: assemble A(kappa), solve with U = [b, g] (the Krylov
+ * basis of b is recomputed, not stored from the forward call), then
+ * dkappa = dL/dkappa (ntri) and, when db is not NULL, db = dL/db = f(A) g (n),
+ * for dL/dx = g.  Pointers as in gm_fe_forward. */
+int gm_fe_backward(gm_handle h, const double* kappa, const double* b, const double* g, double* dkappa, double* db);
 
 /* nsteps steps of the reference's time loop (nicksmethodgpu_problem.m:7-16,
  * nicksmethodgpu_problem_monodomain.m:7-16): build_subspace + lin_sys_solves

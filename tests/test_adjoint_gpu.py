@@ -195,3 +195,25 @@ def test_errors(engine_lib, case2k):
     with pytest.raises(GmError):
         eng.fe_gradient(dk.data_ptr())          # before a solve
     eng.delete()
+
+
+def test_host_pointer_entries(op2k, case2k):
+    """gm_fe_forward / gm_fe_backward (the MEX backward entry) with host
+    buffers give the same bits as with device buffers."""
+    mesh, kappa, b, d = case2k
+    x_dev = op2k.forward(cuda(kappa), cuda(b))
+    dk_dev, db_dev = op2k.backward(cuda(kappa), cuda(b), x_dev - cuda(d))
+    torch.cuda.synchronize()
+    eng = op2k.engine
+    eng.set_stream(None)
+    op2k._stream = None
+    kh, bh = np.ascontiguousarray(kappa), np.ascontiguousarray(b)
+    xh = np.empty_like(bh)
+    eng.fe_forward(kh.ctypes.data, bh.ctypes.data, xh.ctypes.data)
+    gh = xh - d
+    dkh = np.empty(op2k.ntri)
+    dbh = np.empty_like(bh)
+    eng.fe_backward(kh.ctypes.data, bh.ctypes.data, gh.ctypes.data, dkh.ctypes.data, dbh.ctypes.data)
+    np.testing.assert_array_equal(xh, x_dev.cpu().numpy())
+    np.testing.assert_array_equal(dkh, dk_dev.cpu().numpy())
+    np.testing.assert_array_equal(dbh, db_dev.cpu().numpy())
