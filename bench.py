@@ -45,6 +45,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the mixed/batched and oracle checks")
     ap.add_argument("--cpu-sample-s", type=float, default=30.0)
+    ap.add_argument("--threads", type=int, default=0, help="threads per block (0: engine default)")
+    ap.add_argument("--bps", type=int, default=0, help="resident blocks per SM (0: engine default)")
+    ap.add_argument("--diag-compensation", type=int, default=0, choices=[0, 1],
+                    help="mixed engine: 0 = diagonal-compensated FP32 matrix, 1 = plain FP32 values")
     ap.add_argument("--l2-window", type=int, default=0, choices=[0, 1],
                     help="0: keep the SELL matrix in L2 (persisting window), 1: off")
     return ap.parse_args()
@@ -190,7 +194,9 @@ def run_ours(args, P, rank, world, local):
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     R, K, W = args.nrhs, args.steps, args.warmup
-    eng = Engine.from_problem(P, precision=args.precision, sync=False, l2_window=args.l2_window)
+    eng = Engine.from_problem(P, precision=args.precision, sync=False, l2_window=args.l2_window,
+                              threads=args.threads, blocks_per_sm=args.bps,
+                              diag_compensation=args.diag_compensation)
     eng.set_stream(stream.cuda_stream)
     n = P.n
     gen = torch.Generator(device=dev).manual_seed(1234 + rank)

@@ -224,6 +224,22 @@ template <class VT>
 int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp, const std::vector<long long>& prow0,
                 std::vector<long long>& rows, std::vector<long long>& off, std::vector<long long>& pslice0) {
   const int np = (int)prow0.size() - 1;
+  // The mixed engine's diagonal compensation reads x_r from the first gather
+  // of a row, so with compensation every row stores its diagonal entry first
+  // (an explicit zero one where the matrix has none).
+  const bool diag_first = sizeof(VT) == 4 && e->comp;
+  const long long nrows_all = (long long)A.ptr.size() - 1;
+  std::vector<long long> dpos;
+  if (diag_first) {
+    dpos.assign(nrows_all, -1);
+    for (long long r = 0; r < nrows_all; ++r)
+      for (long long t = A.ptr[r]; t < A.ptr[r + 1]; ++t)
+        if (A.col[t] == r) { dpos[r] = t - A.ptr[r]; break; }
+  }
+  auto row_len = [&](long long r) -> long long {
+    const long long len = A.ptr[r + 1] - A.ptr[r];
+    return (diag_first && dpos[r] < 0) ? len + 1 : len;
+  };
   pslice0.assign(np + 1, 0);
   for (int p = 0; p < np; ++p) pslice0[p + 1] = pslice0[p] + (prow0[p + 1] - prow0[p] + 31) / 32;
   const long long nsl = pslice0[np];
@@ -237,7 +253,7 @@ int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp, const std:
       for (long long w0 = 0; w0 < n_p; w0 += sigma) {
         const long long w1 = std::min<long long>(n_p, w0 + sigma);
         std::stable_sort(rp + w0, rp + w1, [&](long long x, long long y) {
-          return (A.ptr[x + 1] - A.ptr[x]) > (A.ptr[y + 1] - A.ptr[y]);
+          return row_len(x) > row_len(y);
         });
       }
     }
@@ -247,7 +263,7 @@ int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp, const std:
     long long L = 0;
     for (int l = 0; l < 32; ++l) {
       const long long r = rows[s * 32 + l];
-      if (r >= 0) L = std::max(L, A.ptr[r + 1] - A.ptr[r]);
+      if (r >= 0) L = std::max(L, row_len(r));
     }
     off[s + 1] = off[s] + 32 * L;
   }
@@ -261,13 +277,26 @@ int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp, const std:
     const long long L = (off[s + 1] - off[s]) / 32;
     for (int l = 0; l < 32; ++l) {
       const long long r = rows[s * 32 + l];
-      const long long len = r >= 0 ? A.ptr[r + 1] - A.ptr[r] : 0;
+      const long long len = r >= 0 ? row_len(r) : 0;
       for (long long jj = 0; jj < L; ++jj) {
         const long long dst = off[s] + jj * 32 + l;
         if (jj < len) {
-          if (e->keep_map) c2s[A.ptr[r] + jj] = (int)dst;
-          col[dst] = A.col[A.ptr[r] + jj];
-          val[dst] = (VT)std::ldexp(A.val[A.ptr[r] + jj], -scale_exp);
+          // entry index within the row: diagonal first when diag_first
+          long long t = jj;
+          bool zero_diag = false;
+          if (diag_first) {
+            const long long dp = dpos[r];
+            if (dp < 0) { zero_diag = jj == 0; t = jj - 1; }
+            else t = jj == 0 ? dp : (jj <= dp ? jj - 1 : jj);
+          }
+          if (zero_diag) {
+            col[dst] = (int)r;
+            val[dst] = (VT)0;
+            continue;
+          }
+          if (e->keep_map) c2s[A.ptr[r] + t] = (int)dst;
+          col[dst] = A.col[A.ptr[r] + t];
+          val[dst] = (VT)std::ldexp(A.val[A.ptr[r] + t], -scale_exp);
         } else {
           col[dst] = r >= 0 ? (int)r : 0;
           val[dst] = (VT)0;
@@ -614,9 +643,9 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
   if (a->keep_entry_map && probs[0].format != GM_CSR) return fail(e, GM_ERR_ARG, "keep_entry_map needs a CSR matrix");
   e->n = ntot; e->nprob = np; e->R = a->nrhs; e->m = a->subspace_size; e->d = a->gamma_size - 1;
   e->C = a->contour_size; e->k = a->num_eigs; e->prec = a->precision; e->sync_mode = a->sync_mode;
-  e->threads = a->threads_per_block ? a->threads_per_block : 512;
-  if (e->threads % 32 || e->threads < 64 || e->threads > 512)
-    return fail(e, GM_ERR_ARG, "threads_per_block must be a multiple of 32 in [64, 512]");
+  e->threads = a->threads_per_block ? a->threads_per_block : GM_MAXT;
+  if (e->threads % 32 || e->threads < 64 || e->threads > GM_MAXT)
+    return fail(e, GM_ERR_ARG, "threads_per_block must be a multiple of 32 in [64, %d]", GM_MAXT);
   GM_CUDA(e, cudaGetDevice(&e->dev));
   GM_CUDA(e, cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, e->dev));
   int coop = 0;

@@ -74,6 +74,12 @@ __device__ __forceinline__ ff ff_from_double(double x) {
 }
 __device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
 
+// L2 prefetch of one global address (no register result, never faults on a
+// valid address; used for the next slice's SELL values).
+__device__ __forceinline__ void prefetch_l2(const void* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // ---------------------------------------------------------------- policies
 struct PolFP64 {
   using VT = double;   // matrix values

@@ -169,6 +169,9 @@ __device__ __forceinline__ long long slot_row(const KParams& kp, long long s, in
 #ifndef GM_CH1
 #define GM_CH1 4
 #endif
+#ifndef GM_PREFETCH_VALS
+#define GM_PREFETCH_VALS 0
+#endif
 #ifndef GM_CH2
 #define GM_CH2 2
 #endif
@@ -194,6 +197,13 @@ __device__ __forceinline__ void spmv_slot(const KParams& kp, long long s, int la
   const VT* vp = reinterpret_cast<const VT*>(kp.val) + base + lane;
 #pragma unroll
   for (int r = 0; r < R; ++r) acc[r] = Pol::zero();
+  // Mixed engine: diagonal compensation of the FP32-stored values, c_r x_r.
+  // The engine stores every row's diagonal entry first (slice column 0), so
+  // x_r is the first chunk's first gather; pad lanes carry dl = 0.
+  float dl = 0.f;
+  if constexpr (Pol::kMixed) {
+    if (kp.dlo) dl = __ldg(kp.dlo + s * 32 + lane);
+  }
   for (int jj = 0; jj < len; jj += CH) {
     int cc[CH];
     VT aa[CH];
@@ -211,25 +221,18 @@ __device__ __forceinline__ void spmv_slot(const KParams& kp, long long s, int la
 #pragma unroll
     for (int u = 0; u < CH; ++u)
       if (jj + u < len) VecIO<R>::ld(x + (long long)cc[u] * R, xv[u]);
+    if constexpr (Pol::kMixed) {
+      if (jj == 0) {
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[r] = Pol::acc(acc[r], dl, xv[0][r]);
+      }
+    }
 #pragma unroll
     for (int u = 0; u < CH; ++u)
       if (jj + u < len) {
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r] = Pol::acc(acc[r], aa[u], xv[u][r]);
       }
-  }
-  if constexpr (Pol::kMixed) {
-    // diagonal compensation of the FP32-stored values (c_r x_r)
-    if (kp.dlo) {
-      const long long row = slot_row(kp, s, lane);
-      if (row >= 0) {
-        const float dl = kp.dlo[s * 32 + lane];
-        XT xr[R];
-        VecIO<R>::ld(x + row * R, xr);
-#pragma unroll
-        for (int r = 0; r < R; ++r) acc[r] = Pol::acc(acc[r], dl, xr[r]);
-      }
-    }
   }
 }
 
@@ -331,7 +334,19 @@ __device__ __forceinline__ void spmv_pass(const KParams& kp, const Ctx& c, ColSt
   int k = 0;
   for (; s < se; s += c.nw, k ^= 1) {
     const long long sn = s + c.nw;
-    if (sn < se) cs.issue(kp, k ^ 1, sn, c.lane);
+    if (sn < se) {
+      cs.issue(kp, k ^ 1, sn, c.lane);
+#if GM_PREFETCH_VALS
+      // the next slice's values into L2 while this slice computes: one request
+      // per 128-byte line of each slice column
+      const long long bn = kp.slice_off[sn];
+      const int ln = (int)((kp.slice_off[sn + 1] - bn) >> 5);
+      constexpr int per_line = 128 / (int)sizeof(typename Pol::VT);
+      if ((c.lane % per_line) == 0)
+        for (int jj = 0; jj < ln; ++jj)
+          prefetch_l2(reinterpret_cast<const typename Pol::VT*>(kp.val) + bn + (long long)jj * 32 + c.lane);
+#endif
+    }
     const int* scol = cs.ready(kp, k, c.lane);
     AT z[R];
     spmv_slot<Pol, R, XT>(kp, s, c.lane, x, z, scol);
@@ -933,7 +948,10 @@ __device__ bool phase_deflate(const KParams& kp, const Ctx& c, int mode) {
 #define GM_MINB 2
 #endif
 template <class Pol, int R, int PH>
-__global__ void __launch_bounds__(512, (R >= 4 ? 1 : GM_MINB)) fab_kernel(KParams kp) {
+#ifndef GM_MAXT
+#define GM_MAXT 512
+#endif
+__global__ void __launch_bounds__(GM_MAXT, (R >= 4 ? 1 : GM_MINB)) fab_kernel(KParams kp) {
   const Ctx c(kp.G);
   GridBar bar{kp.bar, kp.bar + 1, kp.status, (unsigned)kp.G, kp.timeout_ns};
   if (*(volatile int*)kp.status != 0) return;
