@@ -49,6 +49,10 @@ def parse():
     ap.add_argument("--bps", type=int, default=0, help="resident blocks per SM (0: engine default)")
     ap.add_argument("--diag-compensation", type=int, default=0, choices=[0, 1],
                     help="mixed engine: 0 = diagonal-compensated FP32 matrix, 1 = plain FP32 values")
+    ap.add_argument("--col-staging", type=int, default=0, choices=[0, 1],
+                    help="0: stage SELL column indices in shared memory by TMA, 1: off")
+    ap.add_argument("--unfused", action="store_true",
+                    help="step = build_subspace + lin_sys_solves + apply_V (three launches) instead of gm_solve")
     ap.add_argument("--l2-window", type=int, default=0, choices=[0, 1],
                     help="0: keep the SELL matrix in L2 (persisting window), 1: off")
     return ap.parse_args()
@@ -196,7 +200,7 @@ def run_ours(args, P, rank, world, local):
     R, K, W = args.nrhs, args.steps, args.warmup
     eng = Engine.from_problem(P, precision=args.precision, sync=False, l2_window=args.l2_window,
                               threads=args.threads, blocks_per_sm=args.bps,
-                              diag_compensation=args.diag_compensation)
+                              diag_compensation=args.diag_compensation, col_staging=args.col_staging)
     eng.set_stream(stream.cuda_stream)
     n = P.n
     gen = torch.Generator(device=dev).manual_seed(1234 + rank)
@@ -209,7 +213,12 @@ def run_ours(args, P, rank, world, local):
 
     def step(i):
         eng.set_U_device(B[i].data_ptr())
-        eng.solve()
+        if args.unfused:
+            eng.build_subspace()
+            eng.lin_sys_solves()
+            eng.apply_V()
+        else:
+            eng.solve()
 
     with torch.cuda.stream(stream):
         for i in range(W):

@@ -89,15 +89,21 @@ struct KParams {
 };
 
 // ------------------------------------------------------------------ helpers
+// Thread coordinates, recomputed from the special registers on use rather
+// than held in registers across the passes (the kernel is register-bound).
 struct Ctx {
-  int G, b, tid, nt, lane, warp, nw;
-  long long gw, tw, gt, tt;
-  __device__ Ctx(int G_) {
-    G = G_; b = blockIdx.x; tid = threadIdx.x; nt = blockDim.x;
-    lane = tid & 31; warp = tid >> 5; nw = nt >> 5;
-    gw = (long long)b * nw + warp; tw = (long long)G * nw;
-    gt = (long long)b * nt + tid; tt = (long long)G * nt;
-  }
+  int G;
+  __device__ explicit Ctx(int G_) : G(G_) {}
+  __device__ __forceinline__ int b() const { return blockIdx.x; }
+  __device__ __forceinline__ int tid() const { return threadIdx.x; }
+  __device__ __forceinline__ int nt() const { return blockDim.x; }
+  __device__ __forceinline__ int lane() const { return threadIdx.x & 31; }
+  __device__ __forceinline__ int warp() const { return threadIdx.x >> 5; }
+  __device__ __forceinline__ int nw() const { return blockDim.x >> 5; }
+  __device__ __forceinline__ long long gw() const { return (long long)blockIdx.x * nw() + warp(); }
+  __device__ __forceinline__ long long tw() const { return (long long)G * nw(); }
+  __device__ __forceinline__ long long gt() const { return (long long)blockIdx.x * blockDim.x + threadIdx.x; }
+  __device__ __forceinline__ long long tt() const { return (long long)G * blockDim.x; }
 };
 
 __device__ __forceinline__ DepSync make_dep(const KParams& kp) {
@@ -110,17 +116,14 @@ __device__ __forceinline__ DepSync make_dep(const KParams& kp) {
 // numbers keep increasing across phases: a phase that restarted at 0 would
 // find its waits already satisfied by flags published earlier in the launch.
 struct PassSync {
-  GridBar bar;
-  DepSync dep;
   int mode;
+  int p;        // problem (group) whose barrier orders the passes without waits
   unsigned pc;
-  __device__ void done() {
+  __device__ void done(const KParams& kp) {
     ++pc;
-    if (mode) dep.publish(pc);
+    if (mode) make_dep(kp).publish(pc);
   }
-  __device__ bool before_next() {
-    return mode ? dep.wait(pc) : bar.sync();
-  }
+  __device__ bool before_next(const KParams& kp);
 };
 
 // The block's problem group.  A launch can carry several independent
@@ -129,26 +132,37 @@ struct PassSync {
 // single-group case.
 struct Grp {
   int p, gb, Gp, bl;
-  long long r0, r1, gt, tt;
   __device__ Grp(const KParams& kp, const Ctx& c) {
     if (kp.nprob > 0) {
-      p = kp.blk_prob[c.b];
+      p = kp.blk_prob[c.b()];
       gb = kp.prob_blk0[p];
       Gp = kp.prob_blk0[p + 1] - gb;
-      r0 = kp.prob_row0[p];
-      r1 = kp.prob_row0[p + 1];
     } else {
-      p = 0; gb = 0; Gp = c.G; r0 = 0; r1 = kp.n;
+      p = 0; gb = 0; Gp = c.G;
     }
-    bl = c.b - gb;
-    gt = r0 + (long long)bl * c.nt + c.tid;
-    tt = (long long)Gp * c.nt;
+    bl = c.b() - gb;
   }
+  // rows of this problem and the group-strided row loop (recomputed on use)
+  __device__ __forceinline__ long long r0(const KParams& kp) const { return kp.nprob > 0 ? kp.prob_row0[p] : 0; }
+  __device__ __forceinline__ long long r1(const KParams& kp) const { return kp.nprob > 0 ? kp.prob_row0[p + 1] : kp.n; }
+  __device__ __forceinline__ long long gt(const KParams& kp) const {
+    return r0(kp) + (long long)bl * blockDim.x + threadIdx.x;
+  }
+  __device__ __forceinline__ long long tt() const { return (long long)Gp * blockDim.x; }
   // barrier over this group's blocks (words 2 + 2p, 3 + 2p of kp.bar)
   __device__ GridBar bar(const KParams& kp) const {
     return GridBar{kp.bar + 2 + 2 * p, kp.bar + 3 + 2 * p, kp.status, (unsigned)Gp, kp.timeout_ns};
   }
 };
+
+__device__ __forceinline__ GridBar group_bar(const KParams& kp, int p) {
+  const unsigned Gp = kp.nprob > 0 ? (unsigned)(kp.prob_blk0[p + 1] - kp.prob_blk0[p]) : (unsigned)kp.G;
+  return GridBar{kp.bar + 2 + 2 * p, kp.bar + 3 + 2 * p, kp.status, Gp, kp.timeout_ns};
+}
+
+__device__ __forceinline__ bool PassSync::before_next(const KParams& kp) {
+  return mode ? make_dep(kp).wait(pc) : group_bar(kp, p).sync();
+}
 
 // Row of SELL slot (slice s, lane); -1 for padding.
 __device__ __forceinline__ long long slot_row(const KParams& kp, long long s, int lane) {
@@ -247,29 +261,29 @@ template <> __device__ __forceinline__ ff h_load_at<PolMixed>(const float2& h) {
 // gathers together) instead of two.  Dynamic shared memory holds, per warp,
 // two mbarriers and two stages of stage_cap * 32 ints.
 struct ColStage {
-  int* buf0;
-  int* buf1;
-  unsigned long long* bar0;
-  unsigned long long* bar1;
-  unsigned phase;     // bit k: parity of stage k's next completion
-  unsigned issued;    // bit k: stage k holds an outstanding copy
+  unsigned st;   // bit k: parity of stage k's next completion; bit 2 + k: stage k holds a copy
   int cap;
+
+  // stage k's mbarrier and buffer for this warp, derived from the warp index
+  __device__ __forceinline__ static unsigned char* base() {
+    extern __shared__ __align__(128) unsigned char dsm[];
+    return dsm;
+  }
+  __device__ __forceinline__ unsigned long long* bar(int k) const {
+    return reinterpret_cast<unsigned long long*>(base()) + 2 * (threadIdx.x >> 5) + k;
+  }
+  __device__ __forceinline__ int* buf(int k) const {
+    int* bufs = reinterpret_cast<int*>(base() + 16 * (blockDim.x >> 5));
+    return bufs + (long long)(2 * (threadIdx.x >> 5) + k) * cap * 32;
+  }
 
   __device__ void init(const KParams& kp, const Ctx& c) {
     cap = kp.stage_cap;
-    phase = 0u;
-    issued = 0u;
+    st = 0u;
     if (cap <= 0) return;
-    extern __shared__ __align__(128) unsigned char dsm[];
-    unsigned long long* bars = reinterpret_cast<unsigned long long*>(dsm);
-    int* bufs = reinterpret_cast<int*>(dsm + 16 * c.nw);
-    bar0 = bars + 2 * c.warp;
-    bar1 = bar0 + 1;
-    buf0 = bufs + (long long)(2 * c.warp) * cap * 32;
-    buf1 = buf0 + (long long)cap * 32;
-    if (c.lane == 0) {
-      mbar_init(bar0, 1);
-      mbar_init(bar1, 1);
+    if (c.lane() == 0) {
+      mbar_init(bar(0), 1);
+      mbar_init(bar(1), 1);
       mbar_init_fence();
     }
     __syncwarp();
@@ -282,23 +296,23 @@ struct ColStage {
     const int len = (int)((kp.slice_off[s + 1] - base) >> 5);
     if (len <= 0 || len > cap) return;
     if (lane == 0) {
-      unsigned long long* bar = k ? bar1 : bar0;
+      unsigned long long* b = bar(k);
       const unsigned bytes = 128u * (unsigned)len;
-      mbar_arrive_expect_tx(bar, bytes);
-      tma_bulk_g2s(k ? buf1 : buf0, kp.col + base, bytes, bar);
+      mbar_arrive_expect_tx(b, bytes);
+      tma_bulk_g2s(buf(k), kp.col + base, bytes, b);
     }
-    issued |= 1u << k;
+    st |= 4u << k;
   }
 
   // Waits for stage k; returns its buffer, or nullptr when the slice is read
   // from global memory (not staged) or the wait ran out (status recorded).
   __device__ const int* ready(const KParams& kp, int k, int lane) {
-    if (!(issued & (1u << k))) return nullptr;
-    unsigned long long* bar = k ? bar1 : bar0;
-    const unsigned par = (phase >> k) & 1u;
+    if (!(st & (4u << k))) return nullptr;
+    unsigned long long* b = bar(k);
+    const unsigned par = (st >> k) & 1u;
     unsigned long long start = 0;
     bool timed_out = false;
-    while (!mbar_try_wait(bar, par)) {
+    while (!mbar_try_wait(b, par)) {
       const unsigned long long now = global_timer_ns();
       if (start == 0) {
         start = now;
@@ -310,9 +324,9 @@ struct ColStage {
         break;
       }
     }
-    phase ^= 1u << k;
-    issued &= ~(1u << k);
-    return timed_out ? nullptr : (k ? buf1 : buf0);
+    st ^= 1u << k;
+    st &= ~(4u << k);
+    return timed_out ? nullptr : buf(k);
   }
 
   // all lanes are done reading stage k before a later copy overwrites it
@@ -328,28 +342,28 @@ struct ColStage {
 template <class Pol, int R, class XT, class Epi>
 __device__ __forceinline__ void spmv_pass(const KParams& kp, const Ctx& c, ColStage& cs, const XT* x, Epi&& epi) {
   using AT = typename Pol::AT;
-  const long long sb = kp.blk_slice[c.b], se = kp.blk_slice[c.b + 1];
-  long long s = sb + c.warp;
-  if (s < se) cs.issue(kp, 0, s, c.lane);
+  const long long sb = kp.blk_slice[c.b()], se = kp.blk_slice[c.b() + 1];
+  long long s = sb + c.warp();
+  if (s < se) cs.issue(kp, 0, s, c.lane());
   int k = 0;
-  for (; s < se; s += c.nw, k ^= 1) {
-    const long long sn = s + c.nw;
+  for (; s < se; s += c.nw(), k ^= 1) {
+    const long long sn = s + c.nw();
     if (sn < se) {
-      cs.issue(kp, k ^ 1, sn, c.lane);
+      cs.issue(kp, k ^ 1, sn, c.lane());
 #if GM_PREFETCH_VALS
       // the next slice's values into L2 while this slice computes: one request
       // per 128-byte line of each slice column
       const long long bn = kp.slice_off[sn];
       const int ln = (int)((kp.slice_off[sn + 1] - bn) >> 5);
       constexpr int per_line = 128 / (int)sizeof(typename Pol::VT);
-      if ((c.lane % per_line) == 0)
+      if ((c.lane() % per_line) == 0)
         for (int jj = 0; jj < ln; ++jj)
-          prefetch_l2(reinterpret_cast<const typename Pol::VT*>(kp.val) + bn + (long long)jj * 32 + c.lane);
+          prefetch_l2(reinterpret_cast<const typename Pol::VT*>(kp.val) + bn + (long long)jj * 32 + c.lane());
 #endif
     }
-    const int* scol = cs.ready(kp, k, c.lane);
+    const int* scol = cs.ready(kp, k, c.lane());
     AT z[R];
-    spmv_slot<Pol, R, XT>(kp, s, c.lane, x, z, scol);
+    spmv_slot<Pol, R, XT>(kp, s, c.lane(), x, z, scol);
     epi(s, z);
     cs.release();
   }
@@ -400,7 +414,6 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
   using AT = typename Pol::AT;
   const long long n = kp.n;
   const int m = kp.m, d = kp.d, G = kp.G;
-  GridBar bar = g.bar(kp);
   double* const aab = kp.aabb + (long long)(m + 1) * 2 * R * g.p;   // this problem's aabb
   int* const meff = kp.meff + (long long)R * g.p;
   const double* const gam = kp.gamma + (long long)(d + 1) * g.p;
@@ -418,7 +431,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
     double bp[R];
 #pragma unroll
     for (int r = 0; r < R; ++r) bp[r] = 0.0;
-    for (long long i = g.gt; i < g.r1; i += g.tt) {
+    for (long long i = g.gt(kp); i < g.r1(kp); i += g.tt()) {
       double u[R];
       VecIO<R>::ld(kp.U + i * R, u);
       BT wb[R];
@@ -426,11 +439,11 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
       for (int r = 0; r < R; ++r) { bp[r] = fma(u[r], u[r], bp[r]); wb[r] = (BT)u[r]; }
       VecIO<R>::st(W1 + i * R, wb);
     }
-    block_sum_store<R>(bp, part_b + c.b, G);
+    block_sum_store<R>(bp, part_b + c.b(), G);
   }
-  if (!bar.sync()) return false;
+  if (!group_bar(kp, g.p).sync()) return false;
   grid_total_smem<R>(part_b + g.gb, G, g.Gp, sh.tot);
-  if (c.tid == 0) {
+  if (c.tid() == 0) {
     for (int r = 0; r < R; ++r) {
       sh.beta[r] = sqrt(sh.tot[r]);
       sh.broken[r] = !(sh.beta[r] > 0.0);
@@ -460,7 +473,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
     // rounds once to storage (rounding before the subtraction would make the
     // storage error relative to |w| instead of to beta_{j+1} << |w|).
     HT* const Hw = (d & 1) ? H0 : H1;
-    if (c.tid == 0) {
+    if (c.tid() == 0) {
       for (int r = 0; r < R; ++r) {
         sh.sc[r] = Pol::scalar(sh.rbeta[r] * gam[0]);
         sh.rb[r] = Pol::scalar(sh.rbeta[r]);
@@ -474,7 +487,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
     for (int r = 0; r < R; ++r) apa[r] = Pol::zero();
     if (d == 0) {
       spmv_pass<Pol, R, BT>(kp, c, cs, src, [&](long long s, AT (&z)[R]) {
-        const long long row = slot_row(kp, s, c.lane);
+        const long long row = slot_row(kp, s, c.lane());
         if (row < 0) return;
         BT sv[R], v[R];
         VecIO<R>::ld(src + row * R, sv);
@@ -499,7 +512,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
       // Horner pass 1: u = gamma_1 v_j + A (gamma_0 v_j); stores v_j
       {
         spmv_pass<Pol, R, BT>(kp, c, cs, src, [&](long long s, AT (&z)[R]) {
-          const long long row = slot_row(kp, s, c.lane);
+          const long long row = slot_row(kp, s, c.lane());
           if (row < 0) return;
           BT sv[R], v[R];
           VecIO<R>::ld(src + row * R, sv);
@@ -512,13 +525,13 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
           VecIO<R>::st(H1 + row * R, u);
         });
       }
-      ps.done();
-      if (!ps.before_next()) return false;
+      ps.done(kp);
+      if (!ps.before_next(kp)) return false;
       for (int h = 2; h <= d; ++h) {
         const HT* hin = (h & 1) ? H0 : H1;
         HT* hout = (h & 1) ? H1 : H0;
         spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
-          const long long row = slot_row(kp, s, c.lane);
+          const long long row = slot_row(kp, s, c.lane());
           if (row < 0) return;
           BT sv[R];
           VecIO<R>::ld(src + row * R, sv);
@@ -527,13 +540,13 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
           for (int r = 0; r < R; ++r) u[r] = Pol::to_h(Pol::add_mul(z[r], sh.gr[h][r], sv[r]));
           VecIO<R>::st(hout + row * R, u);
         });
-        ps.done();
-        if (!ps.before_next()) return false;
+        ps.done(kp);
+        if (!ps.before_next(kp)) return false;
       }
       // final pass: w = A u - beta_j v_{j-1}
       const HT* hin = (d & 1) ? H1 : H0;
       spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
-        const long long row = slot_row(kp, s, c.lane);
+        const long long row = slot_row(kp, s, c.lane());
         if (row < 0) return;
         BT sv[R];
         VecIO<R>::ld(src + row * R, sv);
@@ -556,12 +569,12 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
       double ap[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) ap[r] = Pol::to_d(apa[r]);
-      block_sum_store<R>(ap, part_a + c.b, G);
+      block_sum_store<R>(ap, part_a + c.b(), G);
     }
-    ps.done();
-    if (!bar.sync()) return false;
+    ps.done(kp);
+    if (!group_bar(kp, g.p).sync()) return false;
     grid_total_smem<R>(part_a + g.gb, G, g.Gp, sh.alpha);
-    if (c.tid == 0) {
+    if (c.tid() == 0) {
       // alpha_j = w^T v_j = rbeta_j (w^T w_j); pass B subtracts alpha_j rbeta_j w_j
       for (int r = 0; r < R; ++r) {
         sh.alpha[r] *= sh.rbeta[r];
@@ -574,7 +587,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
       AT bpa[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) bpa[r] = Pol::zero();
-      for (long long i = g.gt; i < g.r1; i += g.tt) {
+      for (long long i = g.gt(kp); i < g.r1(kp); i += g.tt()) {
         HT wh[R];
         BT wb[R], v[R];
         VecIO<R>::ld(Hw + i * R, wh);
@@ -590,11 +603,11 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
       double bp[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) bp[r] = Pol::to_d(bpa[r]);
-      block_sum_store<R>(bp, part_b + c.b, G);
+      block_sum_store<R>(bp, part_b + c.b(), G);
     }
-    if (!bar.sync()) return false;
+    if (!group_bar(kp, g.p).sync()) return false;
     grid_total_smem<R>(part_b + g.gb, G, g.Gp, sh.tot);
-    if (c.tid == 0) {
+    if (c.tid() == 0) {
       int all = 1;
       for (int r = 0; r < R; ++r) {
         const double bn = sqrt(sh.tot[r]);
@@ -637,8 +650,8 @@ template <int R>
 __device__ void phase_trisolve(const KParams& kp, const Ctx& c) {
   const int m = kp.m, C = kp.C;
   const int np = kp.nprob > 0 ? kp.nprob : 1;
-  if (c.lane != 0) return;
-  for (long long sys = c.gw; sys < (long long)np * R * C; sys += c.tw) {
+  if (c.lane() != 0) return;
+  for (long long sys = c.gw(); sys < (long long)np * R * C; sys += c.tw()) {
     // sys = (p R + r) C + j for problem p, right-hand side r, node j
     const long long rr = sys / C;
     const int j = (int)(sys % C);
@@ -692,7 +705,7 @@ __device__ void phase_coef(const KParams& kp, const Ctx& c) {
   const int m = kp.m, C = kp.C, d1 = kp.d + 1;
   const int np = kp.nprob > 0 ? kp.nprob : 1;
   const long long total = (long long)np * R * d1 * m;
-  for (long long t = c.gt; t < total; t += c.tt) {
+  for (long long t = c.gt(); t < total; t += c.tt()) {
     // t = (rr d1 + i) m + q with rr = p R + r
     const int q = (int)(t % m);
     const int i = (int)((t / m) % d1);
@@ -728,9 +741,9 @@ __device__ bool phase_apply(const KParams& kp, const Ctx& c, const Grp& g, bool 
   HT* const H0 = reinterpret_cast<HT*>(kp.H0);
   HT* const H1 = reinterpret_cast<HT*>(kp.H1);
   constexpr int IC = 3;
-  const long long sb = kp.blk_slice[c.b], se = kp.blk_slice[c.b + 1];
-  for (long long s = sb + c.warp; s < se; s += c.nw) {
-    const long long i = slot_row(kp, s, c.lane);
+  const long long sb = kp.blk_slice[c.b()], se = kp.blk_slice[c.b() + 1];
+  for (long long s = sb + c.warp(); s < se; s += c.nw()) {
+    const long long i = slot_row(kp, s, c.lane());
     if (i < 0) continue;
     for (int i0 = 0; i0 < d1; i0 += IC) {
       AT acc[IC][R];
@@ -784,14 +797,14 @@ __device__ bool phase_apply(const KParams& kp, const Ctx& c, const Grp& g, bool 
     }
   }
   if (d == 0) return true;
-  ps.done();
-  if (!ps.before_next()) return false;
+  ps.done(kp);
+  if (!ps.before_next(kp)) return false;
   for (int h = 1; h <= d; ++h) {
     const HT* hin = h == 1 ? P : ((h & 1) ? H0 : H1);
     HT* hout = (h & 1) ? H1 : H0;
     const HT* Ph = P + (long long)h * n * R;
     spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
-      const long long row = slot_row(kp, s, c.lane);
+      const long long row = slot_row(kp, s, c.lane());
       if (row < 0) return;
       HT p[R];
       VecIO<R>::ld(Ph + row * R, p);
@@ -819,8 +832,8 @@ __device__ bool phase_apply(const KParams& kp, const Ctx& c, const Grp& g, bool 
       }
     });
     if (h < d) {
-      ps.done();
-      if (!ps.before_next()) return false;
+      ps.done(kp);
+      if (!ps.before_next(kp)) return false;
     }
   }
   return true;
@@ -838,7 +851,7 @@ __device__ bool phase_deflate(const KParams& kp, const Ctx& c, int mode) {
   double* part_z = kp.part + 2LL * R * G;
   constexpr int KC = 4;
   if (mode != 0 && R == 2) {
-    for (long long i = c.gt; i < n; i += c.tt) {
+    for (long long i = c.gt(); i < n; i += c.tt()) {
       const double* x = kp.X + i * 2;
       const double* up = kp.upd + i * 2;
       double u = ((x[0] + x[1]) + up[0]) + up[1];
@@ -866,7 +879,7 @@ __device__ bool phase_deflate(const KParams& kp, const Ctx& c, int mode) {
       double zp[KC * R];
 #pragma unroll
       for (int t = 0; t < KC * R; ++t) zp[t] = 0.0;
-      for (long long i = c.gt; i < n; i += c.tt) {
+      for (long long i = c.gt(); i < n; i += c.tt()) {
         double u[R];
         VecIO<R>::ld(kp.Usol + i * R, u);
 #pragma unroll
@@ -878,24 +891,24 @@ __device__ bool phase_deflate(const KParams& kp, const Ctx& c, int mode) {
           }
         }
       }
-      block_sum_store<KC * R>(zp, part_z + (long long)e0 * R * G + c.b, G);
+      block_sum_store<KC * R>(zp, part_z + (long long)e0 * R * G + c.b(), G);
     }
     if (!bar.sync()) return false;
     // every block totals the k*R entries in the same fixed order
     __shared__ double s_z[256];
     const int kr = k * R;
     for (int t0 = 0; t0 < kr; t0 += 256) {
-      for (int t = t0 + c.tid; t < kr && t < t0 + 256; t += c.nt) {
+      for (int t = t0 + c.tid(); t < kr && t < t0 + 256; t += c.nt()) {
         double acc = 0.0;
         const double* p = part_z + (long long)t * G;
         for (int b = 0; b < G; ++b) acc += p[b];
         s_z[t - t0] = acc;
-        if (c.b == 0) kp.Z[t] = acc;
+        if (c.b() == 0) kp.Z[t] = acc;
       }
       __syncthreads();
       // pass 2 over this chunk of Z entries (rows by thread stride)
       const int e_lo = t0 / R, e_hi = min(k, (t0 + 256) / R);
-      for (long long i = c.gt; i < n; i += c.tt) {
+      for (long long i = c.gt(); i < n; i += c.tt()) {
         double u[R], up[R];
         if (t0 == 0) {
           VecIO<R>::ld(kp.Usol + i * R, u);
@@ -927,7 +940,7 @@ __device__ bool phase_deflate(const KParams& kp, const Ctx& c, int mode) {
       __syncthreads();
     }
   } else {
-    for (long long i = c.gt; i < n; i += c.tt) {
+    for (long long i = c.gt(); i < n; i += c.tt()) {
       double u[R], z0[R];
       VecIO<R>::ld(kp.Usol + i * R, u);
 #pragma unroll
@@ -953,17 +966,16 @@ template <class Pol, int R, int PH>
 #endif
 __global__ void __launch_bounds__(GM_MAXT, (R >= 4 ? 1 : GM_MINB)) fab_kernel(KParams kp) {
   const Ctx c(kp.G);
-  GridBar bar{kp.bar, kp.bar + 1, kp.status, (unsigned)kp.G, kp.timeout_ns};
   if (*(volatile int*)kp.status != 0) return;
   const int ph = kp.phases & PH;
   const Grp g(kp, c);
-  PassSync ps{g.bar(kp), make_dep(kp), kp.dep_mode, 0u};
+  PassSync ps{kp.dep_mode, g.p, 0u};
   ColStage cs;
   if (PH & (PH_LANCZOS | PH_APPLY)) cs.init(kp, c);
   bool first = true;
   auto sep = [&]() -> bool {
     if (first) { first = false; return true; }
-    return bar.sync();
+    return GridBar{kp.bar, kp.bar + 1, kp.status, (unsigned)kp.G, kp.timeout_ns}.sync();
   };
   if ((PH & PH_LANCZOS) && (ph & PH_LANCZOS)) {
     if (!sep()) return;
