@@ -728,7 +728,9 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
     int max_persist = 0, max_window = 0;
     GM_CUDA(e, cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, e->dev));
     GM_CUDA(e, cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, e->dev));
-    if (max_persist > 0 && max_window > 0) {
+    // only when the whole matrix fits the persisting set-aside: a partial
+    // window pins a sliver of a large matrix and takes L2 from the vectors
+    if (max_persist > 0 && max_window > 0 && e->mat_bytes <= (size_t)std::min(max_persist, max_window)) {
       const size_t win = std::min<size_t>(e->mat_bytes, (size_t)max_window);
       const size_t setaside = std::min<size_t>(win, (size_t)max_persist);
       GM_CUDA(e, cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, setaside));

@@ -113,8 +113,8 @@ typedef struct gm_create_args {
   int keep_entry_map;          /* 1 = keep the map from stored entries (CSR order)
                                   to device slots, needed by gm_fe_attach          */
   int l2_window;               /* 0 = launches keep the SELL matrix resident in L2
-                                  (persisting access-policy window, up to the
-                                  device's persisting limit; default), 1 = off     */
+                                  (persisting access-policy window) when it fits
+                                  the device's persisting limit (default), 1 = off */
   const double* row_weight;    /* mixed engine, n entries: the FP32-stored matrix
                                   gets a per-row diagonal correction so that
                                   A' w = A w exactly for this w (the operator's
