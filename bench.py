@@ -153,7 +153,8 @@ def host_deflate(P, B):
 
 
 def run_reference(args, P, rank):
-    if rank != 0:
+    from gpumatfun_gb300 import replicas
+    if not replicas.rank0_only(rank):
         return
     from oracle import cpu_fab
     th = cpu_fab.max_threads()
@@ -193,7 +194,7 @@ def config_of(args, P):
 
 def run_ours(args, P, rank, world, local):
     import torch
-    from gpumatfun_gb300 import Engine, roofline
+    from gpumatfun_gb300 import Engine, replicas, roofline
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
@@ -249,10 +250,7 @@ def run_ours(args, P, rank, world, local):
         clocks = clk.stop()
     eng.sync()
     x_last = eng.get_solution()
-    if world > 1:
-        t = torch.tensor([ms_step, ms_fused], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_step, ms_fused = float(t[0]), float(t[1])
+    ms_step, ms_fused = replicas.max_over_ranks([ms_step, ms_fused], device=dev)
     value = world * R * 1e3 / ms_step
 
     # end to end through the C ABI with pinned host buffers
@@ -277,10 +275,7 @@ def run_ours(args, P, rank, world, local):
     torch.cuda.synchronize()
     wall = (time.perf_counter() - w0) / K
     ms_e2e = g0.elapsed_time(g1) / K
-    if world > 1:
-        t = torch.tensor([ms_e2e, wall], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_e2e, wall = float(t[0]), float(t[1])
+    ms_e2e, wall = replicas.max_over_ranks([ms_e2e, wall], device=dev)
     e2e = {"value": world * R * 1e3 / ms_e2e, "unit": "solves/s", "h2d_bytes_per_step": 8 * n * R,
            "d2h_bytes_per_step": 8 * n * R, "host_wall_ms_per_step": wall * 1e3}
 
