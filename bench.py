@@ -380,7 +380,8 @@ def mixed_batched(P, K, W, dev, stream, x_ref_engine=None):
 def run_adjoint(args):
     """Adjoint workload: x = f(A(kappa)) b on the 250k-node FE disk, loss
     L = 1/2 ||x - d||^2, one step = forward + backward (dL/dkappa per
-    triangle and dL/db) through the same calls torch.autograd uses."""
+    triangle and dL/db) through the same calls torch.autograd uses (the
+    backward reuses the forward's stored Krylov state)."""
     import torch
     from gpumatfun_gb300 import adjoint, workloads
     n_target = int(args.workload.split("-")[-1].replace("k", "000"))
@@ -432,7 +433,7 @@ def run_adjoint(args):
     for _ in range(K):
         op.engine.fe_forward(kh.ctypes.data, bh.ctypes.data, xh.ctypes.data)
         gh = xh - dh
-        op.engine.fe_backward(kh.ctypes.data, bh.ctypes.data, gh.ctypes.data, dkh.ctypes.data, dbh.ctypes.data)
+        op.engine.fe_backward_stored(gh.ctypes.data, dkh.ctypes.data, dbh.ctypes.data)
     e2e_s = (time.perf_counter() - t1) / K
     op._stream = None
     dk64, db64, x64 = grads["fp64"]

@@ -23,8 +23,12 @@ The engine kernels behind it:
   shifted solutions of both columns, applies the shifted polynomial, and
   reduces per triangle.
 
-The Krylov basis of b is recomputed in the backward solve rather than stored
-from the forward one. Forward and backward each cost one engine solve.
+By default the operator's engine has one right-hand side, and it keeps the
+forward solve's Krylov state: its basis and shifted solutions. A backward
+call at the same κ and b then costs one more solve, for g.
+`store_basis=False` recomputes that state instead: a two-column engine solves
+[b, g] together. This needs one basis of memory instead of two and costs more
+time.
 
 ``FracFEOperator`` owns one engine for one mesh. ``FracFESolve`` is the
 ``torch.autograd.Function`` over it. The functions act on CUDA float64
@@ -117,7 +121,7 @@ class FracFEOperator:
 
     def __init__(self, mesh: problems.FEMesh, kappa0: np.ndarray, alpha: float = 1.6, m: int = 150,
                  C: int = 32, degree: int = 16, l1: float | None = None, lN: float | None = None,
-                 margin: float = 2.0, precision: str = "fp64", **engine_kw):
+                 margin: float = 2.0, precision: str = "fp64", store_basis: bool = True, **engine_kw):
         self.st = fe_structure(mesh)
         self.alpha = float(alpha)
         self.f = params.frac_power(-alpha / 2)
@@ -135,9 +139,12 @@ class FracFEOperator:
         w = self.contour.weights_mat(self.f)
         self.m, self.C, self.degree = int(m), int(C), int(degree)
         n = self.st.n
-        self.engine = Engine(A0, np.zeros((n, 2)), None, None, None, m, self.gamma, gs.real, gs.imag, [w, w],
-                             params.shifts_vector(sigma, m, 2), col_scale=np.ones(2), precision=precision,
+        R = 1 if store_basis else 2
+        self.store_basis = bool(store_basis)
+        self.engine = Engine(A0, np.zeros((n, R)), None, None, None, m, self.gamma, gs.real, gs.imag, [w] * R,
+                             params.shifts_vector(sigma, m, R), col_scale=np.ones(R), precision=precision,
                              sync=False, keep_entry_map=True, row_weight=self.st.msqrt, **engine_kw)
+        self._fwd_key = None
         st = self.st
         self.engine.fe_attach(st.ntri, st.ent_ptr, st.ent_tri, st.ent_coef, st.tri_nodes, st.tri_kc)
         self.n, self.ntri = n, st.ntri
@@ -161,7 +168,12 @@ class FracFEOperator:
         b = b.detach().to(torch.float64).contiguous()
         x = torch.empty_like(b)
         self.engine.fe_forward(kappa.data_ptr(), b.data_ptr(), x.data_ptr())
+        self._fwd_key = self._key(kappa, b) if self.store_basis else None
         return x
+
+    @staticmethod
+    def _key(kappa, b):
+        return (kappa.data_ptr(), kappa._version, tuple(kappa.shape), b.data_ptr(), b._version, tuple(b.shape))
 
     def backward(self, kappa, b, gx):
         """(dL/dkappa, dL/db) for dL/dx = gx through gm_fe_backward."""
@@ -172,7 +184,11 @@ class FracFEOperator:
         gx = gx.detach().to(torch.float64).contiguous()
         dk = torch.empty(self.ntri, dtype=torch.float64, device=b.device)
         db = torch.empty_like(b)
-        self.engine.fe_backward(kappa.data_ptr(), b.data_ptr(), gx.data_ptr(), dk.data_ptr(), db.data_ptr())
+        if self._fwd_key is not None and self._fwd_key == self._key(kappa, b):
+            self.engine.fe_backward_stored(gx.data_ptr(), dk.data_ptr(), db.data_ptr())
+        else:
+            self.engine.fe_backward(kappa.data_ptr(), b.data_ptr(), gx.data_ptr(), dk.data_ptr(), db.data_ptr())
+            self._fwd_key = self._key(kappa, b) if self.store_basis else None
         return dk, db
 
     def delete(self):

@@ -77,6 +77,12 @@ struct gm_engine {
   double* fe_kc = nullptr;
   double2* fe_buf[6] = {};
   double* fe_kappa = nullptr;    // kappa copied in by gm_fe_forward / gm_fe_backward
+  // nrhs = 1 adjoint engines keep two Krylov states: slot 0 for b (the
+  // forward solve, kept for the backward call), slot 1 for g
+  struct FeSlot { void* V; double* Yr; double* Yi; double* aabb; int* meff; };
+  FeSlot fe_slot[2] = {};
+  int fe_cur = 0;
+  bool fe_fwd_ok = false;        // slot 0 holds the basis of the last gm_fe_forward
   double* fe_dk = nullptr;       // dL/dkappa before it is copied out
   long long* csr_ptr = nullptr;  // device CSR row pointer (kept with csr2sell)
   double2* fe_yb = nullptr;
@@ -1059,6 +1065,7 @@ static int set_U_common(gm_handle h, const double* U, bool on_device) {
   if (!h) return GM_ERR_ARG;
   int rc = set_usol(h, U, on_device);
   if (rc) return rc;
+  if (h->fe_cur == 0) h->fe_fwd_ok = false;   // the stored forward state is being replaced
   GM_CUDA(h, cudaMemsetAsync(h->kp.status, 0, sizeof(int), h->stream));
   GM_CUDA(h, cudaMemsetAsync(h->kp.bar, 0, sizeof(unsigned), h->stream));
   h->have_V = h->have_y = h->have_coef = false;
@@ -1131,6 +1138,7 @@ int gm_fe_assemble(gm_handle h, const double* kappa_dev) {
   GM_CUDA(h, cudaGetLastError());
   h->launches++;
   h->have_V = h->have_y = h->have_coef = false;
+  h->fe_fwd_ok = false;
   return h->sync_mode ? check_sync(h) : GM_OK;
 }
 
@@ -1138,28 +1146,30 @@ int gm_fe_assemble(gm_handle h, const double* kappa_dev) {
 
 namespace {
 // Y -> the lift coefficients of the gradient: yb'[j][q] = y_b,j[q] / w_j
-// (w_j the true weight: the stored one times 2^se) and yg[j][q] = y_g,j[q].
-__global__ void k_fe_prep_y(int C, int m, const double* __restrict__ Yr, const double* __restrict__ Yi,
+// (w_j the true weight: the stored one times 2^se) and yg[j][q] = y_g,j[q];
+// column j of each side's Y (m x C, column-major).
+__global__ void k_fe_prep_y(int C, int m, const double* __restrict__ Yrb, const double* __restrict__ Yib,
+                            const double* __restrict__ Yrg, const double* __restrict__ Yig,
                             const double* __restrict__ wts, int se, double2* __restrict__ yb, double2* __restrict__ yg) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= C * m) return;
   const int j = t / m, q = t % m;
   const double wr = ldexp(wts[j], se), wi = ldexp(wts[C + j], se);
-  const double ar = Yr[(long long)j * m + q], ai = Yi[(long long)j * m + q];
+  const double ar = Yrb[(long long)j * m + q], ai = Yib[(long long)j * m + q];
   const double den = wr * wr + wi * wi;
   yb[t] = make_double2((ar * wr + ai * wi) / den, (ai * wr - ar * wi) / den);
-  yg[t] = make_double2(Yr[(long long)(C + j) * m + q], Yi[(long long)(C + j) * m + q]);
+  yg[t] = make_double2(Yrg[(long long)j * m + q], Yig[(long long)j * m + q]);
 }
 }  // namespace
 
 extern "C" {
 
-int gm_fe_gradient(gm_handle h, double* dkappa_dev) {
-  if (!h || !dkappa_dev) return GM_ERR_ARG;
-  if (!h->fe_nodes) return fail(h, GM_ERR_STATE, "fe_gradient before fe_attach");
-  if (h->R != 2 || h->k != 0 || h->nprob != 1)
-    return fail(h, GM_ERR_UNSUPPORTED, "fe_gradient needs nrhs = 2 (b, g) and no deflation");
-  if (!h->have_y) return fail(h, GM_ERR_STATE, "fe_gradient needs build_subspace and lin_sys_solves for [b, g] first");
+// The gradient from the two Krylov states: Y of b (divided by the weights)
+// and of g, the bases Vb, Vg (element (q, i) at V[(q n + i) vstride]) and
+// their m_eff; then the shifted-polynomial Horner and the per-triangle sum.
+static int fe_gradient_core(gm_handle h, const double* Yrb, const double* Yib, const double* Yrg, const double* Yig,
+                            const void* Vb, const void* Vg, int vstride, const int* meff_b, const int* meff_g,
+                            double* dkappa_dev) {
   const long long n = h->n;
   const int C = h->C, m = h->m, d = h->d;
   int rc;
@@ -1172,20 +1182,20 @@ int gm_fe_gradient(gm_handle h, double* dkappa_dev) {
   }
   double2 *Zb = h->fe_buf[0], *Zg = h->fe_buf[1];
   double2 *Xb[2] = {h->fe_buf[2], h->fe_buf[3]}, *Xg[2] = {h->fe_buf[4], h->fe_buf[5]};
-  k_fe_prep_y<<<(C * m + 255) / 256, 256, 0, h->stream>>>(C, m, h->kp.Yr, h->kp.Yi, h->kp.wts, h->scale_exp,
+  k_fe_prep_y<<<(C * m + 255) / 256, 256, 0, h->stream>>>(C, m, Yrb, Yib, Yrg, Yig, h->kp.wts, h->scale_exp,
                                                            h->fe_yb, h->fe_yg);
   const size_t smem = sizeof(double2) * 2 * 8 * m;
   const unsigned lblocks = (unsigned)std::min<long long>((n + 255) / 256, 8LL * h->nsm);
   if (h->prec == GM_FP64) {
     if (smem > 48 * 1024)
       GM_CUDA(h, cudaFuncSetAttribute(gm::k_fe_lift<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    gm::k_fe_lift<double><<<lblocks, 256, smem, h->stream>>>(n, m, C, (const double*)h->kp.V, h->fe_yb, h->fe_yg,
-                                                             Zb, Zg, h->kp.meff);
+    gm::k_fe_lift<double><<<lblocks, 256, smem, h->stream>>>(n, m, C, (const double*)Vb, (const double*)Vg, vstride,
+                                                             h->fe_yb, h->fe_yg, Zb, Zg, meff_b, meff_g);
   } else {
     if (smem > 48 * 1024)
       GM_CUDA(h, cudaFuncSetAttribute(gm::k_fe_lift<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    gm::k_fe_lift<float><<<lblocks, 256, smem, h->stream>>>(n, m, C, (const float*)h->kp.V, h->fe_yb, h->fe_yg,
-                                                            Zb, Zg, h->kp.meff);
+    gm::k_fe_lift<float><<<lblocks, 256, smem, h->stream>>>(n, m, C, (const float*)Vb, (const float*)Vg, vstride,
+                                                            h->fe_yb, h->fe_yg, Zb, Zg, meff_b, meff_g);
   }
   h->launches += 2;
   // X = gs(0, j) Z; X = A X + gs(i, j) Z for i = 1..d  ->  R_j, S_j
@@ -1206,6 +1216,20 @@ int gm_fe_gradient(gm_handle h, double* dkappa_dev) {
                                                                               Xb[d & 1], Xg[d & 1], dkappa_dev);
   GM_CUDA(h, cudaGetLastError());
   h->launches++;
+  return GM_OK;
+}
+
+int gm_fe_gradient(gm_handle h, double* dkappa_dev) {
+  if (!h || !dkappa_dev) return GM_ERR_ARG;
+  if (!h->fe_nodes) return fail(h, GM_ERR_STATE, "fe_gradient before fe_attach");
+  if (h->R != 2 || h->k != 0 || h->nprob != 1)
+    return fail(h, GM_ERR_UNSUPPORTED, "fe_gradient needs nrhs = 2 (b, g) and no deflation");
+  if (!h->have_y) return fail(h, GM_ERR_STATE, "fe_gradient needs build_subspace and lin_sys_solves for [b, g] first");
+  const int C = h->C, m = h->m;
+  int rc = fe_gradient_core(h, h->kp.Yr, h->kp.Yi, h->kp.Yr + (size_t)C * m, h->kp.Yi + (size_t)C * m, h->kp.V,
+                            static_cast<const char*>(h->kp.V) + (h->prec == GM_FP64 ? sizeof(double) : sizeof(float)),
+                            2, h->kp.meff, h->kp.meff + 1, dkappa_dev);
+  if (rc) return rc;
   return h->sync_mode ? check_sync(h) : GM_OK;
 }
 
@@ -1220,24 +1244,54 @@ static bool host_memory(const void* p) {
 }
 
 // U = [b, g] (g = 0 when null) from host or device memory, via the stage buffer
-static int fe_load(gm_handle h, const double* kappa, const double* b, const double* g) {
-  if (!h->fe_kappa) return fail(h, GM_ERR_STATE, "fe_forward/fe_backward before fe_attach");
-  if (h->R != 2) return fail(h, GM_ERR_UNSUPPORTED, "fe_forward/fe_backward need nrhs = 2");
-  if (!kappa || !b) return fail(h, GM_ERR_ARG, "fe_forward/fe_backward: null kappa or b");
-  const size_t nb = (size_t)h->n * sizeof(double);
-  GM_CUDA(h, cudaMemcpyAsync(h->fe_kappa, kappa, (size_t)h->fe_ntri * sizeof(double), cudaMemcpyDefault, h->stream));
-  int rc = gm_fe_assemble(h, h->fe_kappa);
-  if (rc) return rc;
-  GM_CUDA(h, cudaMemcpyAsync(h->stage, b, nb, cudaMemcpyDefault, h->stream));
-  if (g)
-    GM_CUDA(h, cudaMemcpyAsync(h->stage + h->n, g, nb, cudaMemcpyDefault, h->stream));
-  else
-    GM_CUDA(h, cudaMemsetAsync(h->stage + h->n, 0, nb, h->stream));
-  if ((rc = set_U_common(h, h->stage, true))) return rc;
-  return gm_solve(h);
+// nrhs = 1 adjoint engines: Krylov state slot s (basis, shifted solutions,
+// alpha/beta, m_eff).  Slot 1 is allocated on first use.
+static int fe_use_slot(gm_handle h, int s) {
+  if (!h->fe_slot[0].V) h->fe_slot[0] = {h->kp.V, h->kp.Yr, h->kp.Yi, h->kp.aabb, h->kp.meff};
+  if (s == 1 && !h->fe_slot[1].V) {
+    const size_t bsz = h->prec == GM_FP64 ? sizeof(double) : sizeof(float);
+    unsigned char* V;
+    gm_engine::FeSlot t{};
+    int rc;
+    if ((rc = dalloc(h, &V, (size_t)h->m * h->n * bsz))) return rc;
+    t.V = V;
+    if ((rc = dalloc(h, &t.Yr, (size_t)h->m * h->C))) return rc;
+    if ((rc = dalloc(h, &t.Yi, (size_t)h->m * h->C))) return rc;
+    if ((rc = dalloc(h, &t.aabb, (size_t)(h->m + 1) * 2))) return rc;
+    if ((rc = dalloc(h, &t.meff, 1))) return rc;
+    h->fe_slot[1] = t;
+  }
+  const gm_engine::FeSlot& t = h->fe_slot[s];
+  h->kp.V = t.V; h->kp.Yr = t.Yr; h->kp.Yi = t.Yi; h->kp.aabb = t.aabb; h->kp.meff = t.meff;
+  h->fe_cur = s;
+  return GM_OK;
 }
 
-// column c of the solution (interleaved [n][2]) to dst (host or device)
+// kappa -> A(kappa), then a solve for U (nrhs = 1: b or g into the current
+// slot; nrhs = 2: [b, g], g = 0 when null)
+static int fe_assemble_from(gm_handle h, const double* kappa) {
+  if (!h->fe_kappa) return fail(h, GM_ERR_STATE, "fe_forward/fe_backward before fe_attach");
+  if (!kappa) return fail(h, GM_ERR_ARG, "fe_forward/fe_backward: null kappa");
+  GM_CUDA(h, cudaMemcpyAsync(h->fe_kappa, kappa, (size_t)h->fe_ntri * sizeof(double), cudaMemcpyDefault, h->stream));
+  h->fe_fwd_ok = false;
+  return gm_fe_assemble(h, h->fe_kappa);
+}
+
+static int fe_solve_for(gm_handle h, const double* b, const double* g) {
+  if (!b) return fail(h, GM_ERR_ARG, "fe_forward/fe_backward: null right-hand side");
+  const size_t nb = (size_t)h->n * sizeof(double);
+  GM_CUDA(h, cudaMemcpyAsync(h->stage, b, nb, cudaMemcpyDefault, h->stream));
+  if (h->R == 2) {
+    if (g)
+      GM_CUDA(h, cudaMemcpyAsync(h->stage + h->n, g, nb, cudaMemcpyDefault, h->stream));
+    else
+      GM_CUDA(h, cudaMemsetAsync(h->stage + h->n, 0, nb, h->stream));
+  }
+  int rc = set_U_common(h, h->stage, true);
+  return rc ? rc : gm_solve(h);
+}
+
+// column c of the solution (interleaved [n][R]) to dst (host or device)
 static int fe_store_col(gm_handle h, int c, double* dst) {
   const long long total = h->n * h->R;
   k_pack_out<<<(unsigned)((total + 255) / 256), 256, 0, h->stream>>>(h->kp.S, h->stage, h->n, h->R);
@@ -1248,28 +1302,69 @@ static int fe_store_col(gm_handle h, int c, double* dst) {
   return GM_OK;
 }
 
+static int fe_check(gm_handle h) {
+  if (!h->fe_kappa) return fail(h, GM_ERR_STATE, "fe_forward/fe_backward before fe_attach");
+  if (h->R != 1 && h->R != 2) return fail(h, GM_ERR_UNSUPPORTED, "fe_forward/fe_backward need nrhs = 1 or 2");
+  if (h->k != 0 || h->nprob != 1) return fail(h, GM_ERR_UNSUPPORTED, "fe adjoint: no deflation, one problem");
+  return GM_OK;
+}
+
 int gm_fe_forward(gm_handle h, const double* kappa, const double* b, double* x) {
   if (!h) return GM_ERR_ARG;
   if (!x) return fail(h, GM_ERR_ARG, "fe_forward: null x");
-  int rc = fe_load(h, kappa, b, nullptr);
+  int rc = fe_check(h);
+  if (!rc && h->R == 1) rc = fe_use_slot(h, 0);
+  if (!rc) rc = fe_assemble_from(h, kappa);
+  if (!rc) rc = fe_solve_for(h, b, nullptr);
   if (!rc) rc = fe_store_col(h, 0, x);
   if (rc) return rc;
+  h->fe_fwd_ok = h->R == 1;
   return (h->sync_mode || host_memory(x)) ? check_sync(h) : GM_OK;
+}
+
+// backward with the b state in slot 0 (nrhs = 1) or recomputed with g (nrhs = 2)
+static int fe_backward_impl(gm_handle h, bool reuse, const double* kappa, const double* b, const double* g,
+                            double* dkappa, double* db) {
+  if (!g || !dkappa) return fail(h, GM_ERR_ARG, "fe_backward: null g or dkappa");
+  int rc = fe_check(h);
+  if (rc) return rc;
+  const int saved = h->sync_mode;
+  h->sync_mode = 0;
+  if (h->R == 2) {
+    if (!(rc = fe_assemble_from(h, kappa)) && !(rc = fe_solve_for(h, b, g))) rc = gm_fe_gradient(h, h->fe_dk);
+    if (!rc && db) rc = fe_store_col(h, 1, db);
+  } else {
+    if (!reuse || !h->fe_fwd_ok) {
+      // recompute b's Krylov state into slot 0
+      if (!(rc = fe_use_slot(h, 0)) && !(rc = fe_assemble_from(h, kappa))) rc = fe_solve_for(h, b, nullptr);
+      if (!rc) h->fe_fwd_ok = true;
+    }
+    if (!rc) rc = fe_use_slot(h, 1);
+    if (!rc) rc = fe_solve_for(h, g, nullptr);
+    if (!rc && db) rc = fe_store_col(h, 0, db);
+    if (!rc) {
+      const gm_engine::FeSlot &sb = h->fe_slot[0], &sg = h->fe_slot[1];
+      rc = fe_gradient_core(h, sb.Yr, sb.Yi, sg.Yr, sg.Yi, sb.V, sg.V, 1, sb.meff, sg.meff, h->fe_dk);
+    }
+    const int rc2 = fe_use_slot(h, 0);
+    if (!rc) rc = rc2;
+  }
+  h->sync_mode = saved;
+  if (rc) return rc;
+  GM_CUDA(h, cudaMemcpyAsync(dkappa, h->fe_dk, (size_t)h->fe_ntri * sizeof(double), cudaMemcpyDefault, h->stream));
+  return (h->sync_mode || host_memory(dkappa) || (db && host_memory(db))) ? check_sync(h) : GM_OK;
 }
 
 int gm_fe_backward(gm_handle h, const double* kappa, const double* b, const double* g, double* dkappa, double* db) {
   if (!h) return GM_ERR_ARG;
-  if (!g || !dkappa) return fail(h, GM_ERR_ARG, "fe_backward: null g or dkappa");
-  int rc = fe_load(h, kappa, b, g);
-  if (rc) return rc;
-  const int saved = h->sync_mode;
-  h->sync_mode = 0;
-  rc = gm_fe_gradient(h, h->fe_dk);
-  h->sync_mode = saved;
-  if (rc) return rc;
-  GM_CUDA(h, cudaMemcpyAsync(dkappa, h->fe_dk, (size_t)h->fe_ntri * sizeof(double), cudaMemcpyDefault, h->stream));
-  if (db && (rc = fe_store_col(h, 1, db))) return rc;
-  return (h->sync_mode || host_memory(dkappa) || (db && host_memory(db))) ? check_sync(h) : GM_OK;
+  return fe_backward_impl(h, false, kappa, b, g, dkappa, db);
+}
+
+int gm_fe_backward_stored(gm_handle h, const double* g, double* dkappa, double* db) {
+  if (!h) return GM_ERR_ARG;
+  if (h->R != 1) return fail(h, GM_ERR_UNSUPPORTED, "fe_backward_stored needs an nrhs = 1 engine");
+  if (!h->fe_fwd_ok) return fail(h, GM_ERR_STATE, "fe_backward_stored without a preceding fe_forward");
+  return fe_backward_impl(h, true, nullptr, nullptr, g, dkappa, db);
 }
 
 int gm_time_loop(gm_handle h, int nsteps, int mode, int use_graph) {

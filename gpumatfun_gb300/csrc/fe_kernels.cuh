@@ -66,12 +66,14 @@ __global__ void k_fe_assemble_rows(long long n, const long long* __restrict__ pt
 // (complex; yb' = y_b / w); rows by thread, shifts in chunks of JC whose
 // coefficients sit in shared memory.
 template <class BT>
-__global__ void k_fe_lift(long long n, int m, int C, const BT* __restrict__ V, const double2* __restrict__ yb,
-                          const double2* __restrict__ yg, double2* __restrict__ Rout, double2* __restrict__ Sout,
-                          const int* __restrict__ meff) {
+__global__ void k_fe_lift(long long n, int m, int C, const BT* __restrict__ Vb, const BT* __restrict__ Vg, int vstride,
+                          const double2* __restrict__ yb, const double2* __restrict__ yg, double2* __restrict__ Rout,
+                          double2* __restrict__ Sout, const int* __restrict__ meff_b, const int* __restrict__ meff_g) {
+  // V element (q, i) of a side at V[(q n + i) vstride]: the b and g bases are
+  // columns of one interleaved engine basis, or two separate bases
   constexpr int JC = 8;
   extern __shared__ double2 sy[];  // [2][JC][m]
-  const int mb = min(meff[0], m), mg = min(meff[1], m);
+  const int mb = min(*meff_b, m), mg = min(*meff_g, m);
   for (int j0 = 0; j0 < C; j0 += JC) {
     __syncthreads();
     for (int t = threadIdx.x; t < 2 * JC * m; t += blockDim.x) {
@@ -86,8 +88,8 @@ __global__ void k_fe_lift(long long n, int m, int C, const BT* __restrict__ V, c
 #pragma unroll
       for (int jj = 0; jj < JC; ++jj) { ra[jj] = make_double2(0.0, 0.0); sa[jj] = make_double2(0.0, 0.0); }
       for (int q = 0; q < m; ++q) {
-        const double vb = q < mb ? (double)V[((long long)q * n + i) * 2] : 0.0;
-        const double vg = q < mg ? (double)V[((long long)q * n + i) * 2 + 1] : 0.0;
+        const double vb = q < mb ? (double)Vb[((long long)q * n + i) * vstride] : 0.0;
+        const double vg = q < mg ? (double)Vg[((long long)q * n + i) * vstride] : 0.0;
 #pragma unroll
         for (int jj = 0; jj < JC; ++jj) {
           const double2 b = sy[jj * m + q];

@@ -35,6 +35,7 @@ EXPORTED_SYMBOLS = [
     "gm_phase_times", "gm_info", "gm_get_meff", "gm_last_error", "gm_version",
     "gm_lin_sys_solves_noalloc", "gm_batch_create", "gm_time_loop", "gm_fe_attach", "gm_fe_assemble",
     "gm_fe_gradient", "gm_get_solution_device", "gm_fe_forward", "gm_fe_backward",
+    "gm_fe_backward_stored",
 ]
 
 _dp = ct.POINTER(ct.c_double)
@@ -112,6 +113,7 @@ def load_library(build_if_missing: bool = False) -> ct.CDLL:
     lib.gm_get_solution_device.argtypes = [h, ct.c_void_p]
     lib.gm_fe_forward.argtypes = [h, ct.c_void_p, ct.c_void_p, ct.c_void_p]
     lib.gm_fe_backward.argtypes = [h, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_void_p]
+    lib.gm_fe_backward_stored.argtypes = [h, ct.c_void_p, ct.c_void_p, ct.c_void_p]
     lib.gm_phase_times.argtypes = [h, ct.POINTER(ct.c_float)]
     lib.gm_info.argtypes = [h, _lp]
     lib.gm_get_meff.argtypes = [h, ct.POINTER(ct.c_int)]
@@ -315,6 +317,12 @@ class Engine:
         """dL/dkappa and dL/db for dL/dx = g; arguments are pointers (host or device)."""
         self._check(self._lib.gm_fe_backward(self._h, ct.c_void_p(kappa), ct.c_void_p(b), ct.c_void_p(g),
                                              ct.c_void_p(dkappa), ct.c_void_p(db or 0)))
+
+    def fe_backward_stored(self, g: int, dkappa: int, db: int | None):
+        """Backward at the kappa and b of the last fe_forward (nrhs = 1 engine),
+        reusing its stored Krylov state."""
+        self._check(self._lib.gm_fe_backward_stored(self._h, ct.c_void_p(g), ct.c_void_p(dkappa),
+                                                    ct.c_void_p(db or 0)))
 
     def get_update(self) -> np.ndarray:
         return self._out(self._lib.gm_get_update)

@@ -253,17 +253,25 @@ int gm_fe_assemble(gm_handle h, const double* kappa_dev);
  * dL/db = f(A) g is column 1 of the solution. */
 int gm_fe_gradient(gm_handle h, double* dkappa_dev);
 
-/* One forward evaluation x = f(A(kappa)) b: assemble, solve with U = [b, 0],
- * copy column 0.  kappa (ntri), b and x (n) may be host or device memory
- * (UVA); results in host memory are complete on return, device results
- * follow the handle's stream order. */
+/* One forward evaluation x = f(A(kappa)) b: assemble A(kappa), solve, copy
+ * the solution.  kappa (ntri), b and x (n) may be host or device memory (UVA);
+ * results in host memory are complete on return, device results follow the
+ * handle's stream order.  An nrhs = 1 engine keeps this solve's Krylov state
+ * (basis and shifted solutions) for gm_fe_backward_stored; an nrhs = 2 engine
+ * solves [b, 0]. */
 int gm_fe_forward(gm_handle h, const double* kappa, const double* b, double* x);
 
-/* The backward entry: assemble A(kappa), solve with U = [b, g] (the Krylov
- * basis of b is recomputed, not stored from the forward call), then
- * dkappa = dL/dkappa (ntri) and, when db is not NULL, db = dL/db = f(A) g (n),
- * for dL/dx = g.  Pointers as in gm_fe_forward. */
+/* The backward entry: dkappa = dL/dkappa (ntri) and, when db is not NULL,
+ * db = dL/db = f(A) g (n), for dL/dx = g at x = f(A(kappa)) b.  The Krylov
+ * state of b is recomputed (nrhs = 1: b, then g, in two stored states;
+ * nrhs = 2: [b, g] in one solve).  Pointers as in gm_fe_forward. */
 int gm_fe_backward(gm_handle h, const double* kappa, const double* b, const double* g, double* dkappa, double* db);
+
+/* The same for the kappa and b of the last gm_fe_forward on this nrhs = 1
+ * handle, reusing its stored Krylov state: one solve (for g) instead of two.
+ * GM_ERR_STATE when no forward state is stored (after gm_fe_assemble, gm_set_U
+ * or a forward on another input). */
+int gm_fe_backward_stored(gm_handle h, const double* g, double* dkappa, double* db);
 
 /* nsteps steps of the reference's time loop (nicksmethodgpu_problem.m:7-16,
  * nicksmethodgpu_problem_monodomain.m:7-16): build_subspace + lin_sys_solves

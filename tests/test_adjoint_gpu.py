@@ -76,17 +76,22 @@ def test_gpu_assembly_matches_host(op2k, case2k):
     x_gpu = op2k.forward(cuda(k2), cuda(b)).cpu().numpy()
     # an engine created from the host-assembled A(k2) with the same method parameters
     op_h = adjoint.FracFEOperator(mesh, k2, alpha=ALPHA, m=M2K, C=32, degree=8, l1=op2k.l1, lN=op2k.lN)
-    op_h.engine.set_U(np.stack([b, np.zeros_like(b)], axis=1))
+    U = np.zeros((b.size, op_h.engine.R))
+    U[:, 0] = b
+    op_h.engine.set_U(U)
     op_h.engine.solve()
     x_host = op_h.engine.get_solution()[:, 0]
     op_h.delete()
     assert rel(x_gpu, x_host) < 1e-13
 
 
-def test_gradient_matches_krylov_restatement(engine_lib):
-    """Kernel parity: same Krylov state, same formula, FP64 on the host."""
+@pytest.mark.parametrize("store_basis", [True, False])
+def test_gradient_matches_krylov_restatement(engine_lib, store_basis):
+    """Kernel parity: same Krylov state, same formula, FP64 on the host.
+    store_basis: a one-column engine with two stored Krylov states (b, g);
+    otherwise a two-column engine solving [b, g] together."""
     mesh, kappa, b, d = make_case(500, seed=4)
-    op = adjoint.FracFEOperator(mesh, kappa, alpha=ALPHA, m=30, C=24, degree=3)
+    op = adjoint.FracFEOperator(mesh, kappa, alpha=ALPHA, m=30, C=24, degree=3, store_basis=store_basis)
     x = op.forward(cuda(kappa), cuda(b)).cpu().numpy()
     g = x - d
     dk, db = op.backward(cuda(kappa), cuda(b), cuda(g))
@@ -217,3 +222,23 @@ def test_host_pointer_entries(op2k, case2k):
     np.testing.assert_array_equal(xh, x_dev.cpu().numpy())
     np.testing.assert_array_equal(dkh, dk_dev.cpu().numpy())
     np.testing.assert_array_equal(dbh, db_dev.cpu().numpy())
+
+
+def test_stored_forward_state_is_reused(op2k, case2k):
+    """backward at the forward's kappa and b reuses the stored Krylov state
+    (one solve instead of two) and gives the same bits as recomputing it."""
+    mesh, kappa, b, d = case2k
+    kt, bt = cuda(kappa), cuda(b)
+    x = op2k.forward(kt, bt)
+    launches0 = op2k.engine.info()["launches"]
+    dk1, db1 = op2k.backward(kt, bt, x - cuda(d))          # same tensors: stored state
+    used_stored = op2k.engine.info()["launches"] - launches0
+    dk2, db2 = op2k.backward(cuda(kappa), cuda(b), x - cuda(d))   # new tensors: recomputed
+    used_full = op2k.engine.info()["launches"] - launches0 - used_stored
+    assert used_stored < used_full
+    assert torch.equal(dk1, dk2) and torch.equal(db1, db2)
+    # a fresh forward on other inputs invalidates the stored state
+    op2k.forward(cuda(kappa * 1.01), bt)
+    with pytest.raises(GmError):
+        op2k.engine.fe_assemble(cuda(kappa).data_ptr())
+        op2k.engine.fe_backward_stored((x - cuda(d)).data_ptr(), dk1.data_ptr(), db1.data_ptr())
