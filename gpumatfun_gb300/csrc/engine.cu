@@ -1184,19 +1184,13 @@ static int fe_gradient_core(gm_handle h, const double* Yrb, const double* Yib, c
   double2 *Xb[2] = {h->fe_buf[2], h->fe_buf[3]}, *Xg[2] = {h->fe_buf[4], h->fe_buf[5]};
   k_fe_prep_y<<<(C * m + 255) / 256, 256, 0, h->stream>>>(C, m, Yrb, Yib, Yrg, Yig, h->kp.wts, h->scale_exp,
                                                            h->fe_yb, h->fe_yg);
-  const size_t smem = sizeof(double2) * 2 * 8 * m;
-  const unsigned lblocks = (unsigned)std::min<long long>((n + 255) / 256, 8LL * h->nsm);
-  if (h->prec == GM_FP64) {
-    if (smem > 48 * 1024)
-      GM_CUDA(h, cudaFuncSetAttribute(gm::k_fe_lift<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    gm::k_fe_lift<double><<<lblocks, 256, smem, h->stream>>>(n, m, C, (const double*)Vb, (const double*)Vg, vstride,
+  const unsigned lblocks = (unsigned)std::min<long long>((n + 255) / 256, 2LL * h->nsm);
+  if (h->prec == GM_FP64)
+    gm::k_fe_lift_ff<double><<<lblocks, 256, 0, h->stream>>>(n, m, C, (const double*)Vb, (const double*)Vg, vstride,
                                                              h->fe_yb, h->fe_yg, Zb, Zg, meff_b, meff_g);
-  } else {
-    if (smem > 48 * 1024)
-      GM_CUDA(h, cudaFuncSetAttribute(gm::k_fe_lift<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    gm::k_fe_lift<float><<<lblocks, 256, smem, h->stream>>>(n, m, C, (const float*)Vb, (const float*)Vg, vstride,
+  else
+    gm::k_fe_lift_ff<float><<<lblocks, 256, 0, h->stream>>>(n, m, C, (const float*)Vb, (const float*)Vg, vstride,
                                                             h->fe_yb, h->fe_yg, Zb, Zg, meff_b, meff_g);
-  }
   h->launches += 2;
   // X = gs(0, j) Z; X = A X + gs(i, j) Z for i = 1..d  ->  R_j, S_j
   const unsigned hblocks = (unsigned)std::min<long long>((n + 7) / 8, 32LL * h->nsm);

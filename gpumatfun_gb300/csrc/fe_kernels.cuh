@@ -62,49 +62,85 @@ __global__ void k_fe_assemble_rows(long long n, const long long* __restrict__ pt
   dlo[row2slot[r]] = (float)(corr / w[r]);
 }
 
-// Zb[i][j] = sum_q V[q][i][0] yb'[j][q], Zg[i][j] = sum_q V[q][i][1] yg[j][q]
-// (complex; yb' = y_b / w); rows by thread, shifts in chunks of JC whose
-// coefficients sit in shared memory.
+// The same lift in float-float arithmetic on the FP32 pipe (GB300's FP64
+// pipe issues about 1/64 of its FP32 rate).  Each V element is split into
+// hi + lo floats once and each coefficient is kept split in shared memory;
+// products are exact (two_prod) with the cross terms added, sums compensated:
+// about 48 significant bits, against m-term sums of order 1e3 terms.
+__device__ __forceinline__ ff ff_madd(ff acc, float ah, float al, float bh, float bl) {
+  ff p = two_prod(ah, bh);
+  p.lo = fmaf(ah, bl, fmaf(al, bh, p.lo));
+  ff s = two_sum(acc.hi, p.hi);
+  const float e = s.lo + (acc.lo + p.lo);
+  return fast_two_sum(s.hi, e);
+}
+
 template <class BT>
-__global__ void k_fe_lift(long long n, int m, int C, const BT* __restrict__ Vb, const BT* __restrict__ Vg, int vstride,
-                          const double2* __restrict__ yb, const double2* __restrict__ yg, double2* __restrict__ Rout,
-                          double2* __restrict__ Sout, const int* __restrict__ meff_b, const int* __restrict__ meff_g) {
-  // V element (q, i) of a side at V[(q n + i) vstride]: the b and g bases are
-  // columns of one interleaved engine basis, or two separate bases
-  constexpr int JC = 8;
-  extern __shared__ double2 sy[];  // [2][JC][m]
+__global__ void __launch_bounds__(256) k_fe_lift_ff(long long n, int m, int C, const BT* __restrict__ Vb,
+                                                    const BT* __restrict__ Vg, int vstride,
+                                                    const double2* __restrict__ yb, const double2* __restrict__ yg,
+                                                    double2* __restrict__ Rout, double2* __restrict__ Sout,
+                                                    const int* __restrict__ meff_b, const int* __restrict__ meff_g) {
+  // Zb[i][j] = sum_q Vb(q, i) yb'[j][q], Zg[i][j] = sum_q Vg(q, i) yg[j][q];
+  // V element (q, i) of a side at V[(q n + i) vstride] (the b and g bases are
+  // columns of one interleaved basis, or two separate bases).  One row per
+  // thread; shifts in chunks of JC, coefficients in tiles of QT Krylov
+  // vectors held split in shared memory.
+  constexpr int JC = 8, QT = 128;
+  __shared__ float4 sy4[2 * JC * QT];  // [side][jj][q]: (re hi, re lo, im hi, im lo)
   const int mb = min(*meff_b, m), mg = min(*meff_g, m);
-  for (int j0 = 0; j0 < C; j0 += JC) {
-    __syncthreads();
-    for (int t = threadIdx.x; t < 2 * JC * m; t += blockDim.x) {
-      const int side = t / (JC * m), rest = t % (JC * m), jj = rest / m, q = rest % m;
-      const int j = j0 + jj;
-      const double2* src = side ? yg : yb;
-      sy[t] = (j < C) ? src[(long long)j * m + q] : make_double2(0.0, 0.0);
-    }
-    __syncthreads();
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-      double2 ra[JC], sa[JC];
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i0 = (long long)blockIdx.x * blockDim.x; i0 < n; i0 += stride) {   // block-uniform
+    const long long i = i0 + threadIdx.x;
+    const bool act = i < n;
+    for (int j0 = 0; j0 < C; j0 += JC) {
+      ff rr[JC], ri[JC], sr[JC], si[JC];
 #pragma unroll
-      for (int jj = 0; jj < JC; ++jj) { ra[jj] = make_double2(0.0, 0.0); sa[jj] = make_double2(0.0, 0.0); }
-      for (int q = 0; q < m; ++q) {
-        const double vb = q < mb ? (double)Vb[((long long)q * n + i) * vstride] : 0.0;
-        const double vg = q < mg ? (double)Vg[((long long)q * n + i) * vstride] : 0.0;
+      for (int jj = 0; jj < JC; ++jj) rr[jj] = ri[jj] = sr[jj] = si[jj] = ff{0.f, 0.f};
+      for (int q0 = 0; q0 < m; q0 += QT) {
+        const int qn = min(QT, m - q0);
+        __syncthreads();
+        for (int t = threadIdx.x; t < 2 * JC * QT; t += blockDim.x) {
+          const int side = t / (JC * QT), rest = t % (JC * QT), jj = rest / QT, q = rest % QT;
+          const int j = j0 + jj;
+          const double2* src = side ? yg : yb;
+          const double2 y = (j < C && q < qn) ? src[(long long)j * m + q0 + q] : make_double2(0.0, 0.0);
+          const float rh = (float)y.x, ih = (float)y.y;
+          sy4[t] = make_float4(rh, (float)(y.x - (double)rh), ih, (float)(y.y - (double)ih));
+        }
+        __syncthreads();
+        if (!act) continue;
+        for (int q = 0; q < qn; ++q) {
+          const int qq = q0 + q;
+          float bh = 0.f, bl = 0.f, gh = 0.f, gl = 0.f;
+          if (qq < mb) {
+            const BT v = Vb[((long long)qq * n + i) * vstride];
+            bh = (float)v;
+            bl = (float)(v - (BT)bh);
+          }
+          if (qq < mg) {
+            const BT v = Vg[((long long)qq * n + i) * vstride];
+            gh = (float)v;
+            gl = (float)(v - (BT)gh);
+          }
 #pragma unroll
-        for (int jj = 0; jj < JC; ++jj) {
-          const double2 b = sy[jj * m + q];
-          const double2 g = sy[JC * m + jj * m + q];
-          ra[jj].x = fma(vb, b.x, ra[jj].x);
-          ra[jj].y = fma(vb, b.y, ra[jj].y);
-          sa[jj].x = fma(vg, g.x, sa[jj].x);
-          sa[jj].y = fma(vg, g.y, sa[jj].y);
+          for (int jj = 0; jj < JC; ++jj) {
+            const float4 b = sy4[jj * QT + q];
+            const float4 g = sy4[JC * QT + jj * QT + q];
+            rr[jj] = ff_madd(rr[jj], bh, bl, b.x, b.y);
+            ri[jj] = ff_madd(ri[jj], bh, bl, b.z, b.w);
+            sr[jj] = ff_madd(sr[jj], gh, gl, g.x, g.y);
+            si[jj] = ff_madd(si[jj], gh, gl, g.z, g.w);
+          }
         }
       }
+      if (act) {
 #pragma unroll
-      for (int jj = 0; jj < JC; ++jj) {
-        if (j0 + jj < C) {
-          Rout[i * C + j0 + jj] = ra[jj];
-          Sout[i * C + j0 + jj] = sa[jj];
+        for (int jj = 0; jj < JC; ++jj) {
+          if (j0 + jj < C) {
+            Rout[i * C + j0 + jj] = make_double2(ff_to_double(rr[jj]), ff_to_double(ri[jj]));
+            Sout[i * C + j0 + jj] = make_double2(ff_to_double(sr[jj]), ff_to_double(si[jj]));
+          }
         }
       }
     }
