@@ -1,7 +1,7 @@
 """FP64 numpy restatement of GPUMatfun's f(A)b engine (test infrastructure).
 
-This module is the checker: only tests, ``__graft_entry__.smoke()`` and the
-CPU-baseline leg of ``bench.py`` use it.  Every function follows the
+This module is the oracle the engine is checked against: only tests,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` use it.  Every function follows the
 reference statement by statement and cites it.
 
 Notation (the reference's, lanczos.h:24-86): n rows, m = Krylov dimension

@@ -1,7 +1,7 @@
 """GPU parity of the CUDA engine against the FP64 oracle (through the C ABI).
 
-Tolerances: FP64 engine vs FP64 oracle 1e-10 relative (the spec FP64
-bar); mixed engine vs FP64 oracle 1e-6 relative.  Sizes are such that the
+Tolerances: FP64 engine vs FP64 oracle 1e-10 relative (the FP64 parity
+tolerance); mixed engine vs FP64 oracle 1e-6 relative.  Sizes are such that the
 oracle finishes in well under a second per case.
 """
 import numpy as np
