@@ -183,9 +183,6 @@ __device__ __forceinline__ long long slot_row(const KParams& kp, long long s, in
 #ifndef GM_CH1
 #define GM_CH1 4
 #endif
-#ifndef GM_PREFETCH_VALS
-#define GM_PREFETCH_VALS 0
-#endif
 #ifndef GM_CH2
 #define GM_CH2 2
 #endif
@@ -340,33 +337,29 @@ struct ColStage {
 // One SpMV pass over the block's slices: z = A x for the slice rows, then
 // epi(s, z) for the row epilogue.
 template <class Pol, int R, class XT, class Epi>
-__device__ __forceinline__ void spmv_pass(const KParams& kp, const Ctx& c, ColStage& cs, const XT* x, Epi&& epi) {
+__device__ __forceinline__ bool spmv_pass(const KParams& kp, const Ctx& c, ColStage& cs, const XT* x, Epi&& epi,
+                                          PassSync* wait = nullptr) {
   using AT = typename Pol::AT;
   const long long sb = kp.blk_slice[c.b()], se = kp.blk_slice[c.b() + 1];
   long long s = sb + c.warp();
   if (s < se) cs.issue(kp, 0, s, c.lane());
+  // the ordering wait on the previous pass comes after the first column copy
+  // is issued: the matrix does not depend on it, so the copy overlaps the wait
+  if (wait && !wait->before_next(kp)) {
+    if (s < se) cs.ready(kp, 0, c.lane());   // bounded drain of the copy in flight
+    return false;
+  }
   int k = 0;
   for (; s < se; s += c.nw(), k ^= 1) {
     const long long sn = s + c.nw();
-    if (sn < se) {
-      cs.issue(kp, k ^ 1, sn, c.lane());
-#if GM_PREFETCH_VALS
-      // the next slice's values into L2 while this slice computes: one request
-      // per 128-byte line of each slice column
-      const long long bn = kp.slice_off[sn];
-      const int ln = (int)((kp.slice_off[sn + 1] - bn) >> 5);
-      constexpr int per_line = 128 / (int)sizeof(typename Pol::VT);
-      if ((c.lane() % per_line) == 0)
-        for (int jj = 0; jj < ln; ++jj)
-          prefetch_l2(reinterpret_cast<const typename Pol::VT*>(kp.val) + bn + (long long)jj * 32 + c.lane());
-#endif
-    }
+    if (sn < se) cs.issue(kp, k ^ 1, sn, c.lane());
     const int* scol = cs.ready(kp, k, c.lane());
     AT z[R];
     spmv_slot<Pol, R, XT>(kp, s, c.lane(), x, z, scol);
     epi(s, z);
     cs.release();
   }
+  return true;
 }
 
 // ------------------------------------------------------------------ LANCZOS
@@ -526,11 +519,10 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
         });
       }
       ps.done(kp);
-      if (!ps.before_next(kp)) return false;
       for (int h = 2; h <= d; ++h) {
         const HT* hin = (h & 1) ? H0 : H1;
         HT* hout = (h & 1) ? H1 : H0;
-        spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
+        const bool ok = spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
           const long long row = slot_row(kp, s, c.lane());
           if (row < 0) return;
           BT sv[R];
@@ -539,13 +531,13 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
 #pragma unroll
           for (int r = 0; r < R; ++r) u[r] = Pol::to_h(Pol::add_mul(z[r], sh.gr[h][r], sv[r]));
           VecIO<R>::st(hout + row * R, u);
-        });
+        }, &ps);
+        if (!ok) return false;
         ps.done(kp);
-        if (!ps.before_next(kp)) return false;
       }
       // final pass: w = A u - beta_j v_{j-1}
       const HT* hin = (d & 1) ? H1 : H0;
-      spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
+      const bool ok = spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
         const long long row = slot_row(kp, s, c.lane());
         if (row < 0) return;
         BT sv[R];
@@ -563,7 +555,8 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
 #pragma unroll
         for (int r = 0; r < R; ++r) { wh[r] = Pol::to_h(w[r]); apa[r] = Pol::dot(apa[r], w[r], sv[r]); }
         VecIO<R>::st(Hw + row * R, wh);
-      });
+      }, &ps);
+      if (!ok) return false;
     }
     {
       double ap[R];
@@ -798,12 +791,11 @@ __device__ bool phase_apply(const KParams& kp, const Ctx& c, const Grp& g, bool 
   }
   if (d == 0) return true;
   ps.done(kp);
-  if (!ps.before_next(kp)) return false;
   for (int h = 1; h <= d; ++h) {
     const HT* hin = h == 1 ? P : ((h & 1) ? H0 : H1);
     HT* hout = (h & 1) ? H1 : H0;
     const HT* Ph = P + (long long)h * n * R;
-    spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
+    const bool ok = spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
       const long long row = slot_row(kp, s, c.lane());
       if (row < 0) return;
       HT p[R];
@@ -830,11 +822,9 @@ __device__ bool phase_apply(const KParams& kp, const Ctx& c, const Grp& g, bool 
         VecIO<R>::st(kp.X + row * R, xo);
         VecIO<R>::st(kp.S + row * R, so);
       }
-    });
-    if (h < d) {
-      ps.done(kp);
-      if (!ps.before_next(kp)) return false;
-    }
+    }, &ps);
+    if (!ok) return false;
+    if (h < d) ps.done(kp);
   }
   return true;
 }
