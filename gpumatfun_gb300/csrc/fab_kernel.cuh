@@ -257,6 +257,11 @@ template <> __device__ __forceinline__ ff h_load_at<PolMixed>(const float2& h) {
 // the current slice, so a slice costs one global round trip (values and x
 // gathers together) instead of two.  Dynamic shared memory holds, per warp,
 // two mbarriers and two stages of stage_cap * 32 ints.
+// After a timed-out wait, how long a warp still waits for its TMA copy in
+// flight before leaving (independent of the configured wait limit, which
+// may be short): a copy completes in microseconds unless the GPU is failing.
+constexpr unsigned long long kDrainNs = 2000000000ull;
+
 struct ColStage {
   unsigned st;   // bit k: parity of stage k's next completion; bit 2 + k: stage k holds a copy
   int cap;
@@ -317,7 +322,7 @@ struct ColStage {
         if (lane == 0) atomicCAS(kp.status, 0, (int)ST_TIMEOUT);
         timed_out = true;
         start = now;  // keep waiting a bounded time for the copy in flight
-      } else if (timed_out && now - start > kp.timeout_ns) {
+      } else if (timed_out && now - start > kDrainNs) {
         break;
       }
     }

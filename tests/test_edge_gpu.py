@@ -121,3 +121,26 @@ def test_autotune_on_gpu(engine_lib, tmp_path):
     eng.solve()
     assert rel(eng.get_solution(), oracle(P)) < 1e-10
     eng.delete()
+
+
+def test_wait_limit_reports_timeout_and_context_survives(engine_lib):
+    """Failure detection without a GPU fault: with a 100 ns wait limit the
+    bounded barrier and neighbour waits of a many-block launch run out; the
+    kernel records GM_ERR_TIMEOUT and returns, the host reads the status, and
+    the same context (and the same handle after gm_set_U) solves normally."""
+    from gpumatfun_gb300.engine import GmError
+    P = workloads.fd2d_problem(160, 0, 16, 12, [params.frac_exp(1e-3, 1.5)], R=1, scale=161.0 ** 2, seed=1)
+    want = oracle(P)
+    eng = None
+    with pytest.raises(GmError) as err:
+        # the create-time deflation launch may already run out; otherwise a solve does
+        eng = Engine.from_problem(P, timeout_s=1e-7, threads=128, sync=True)
+        for _ in range(20):           # a launch whose every wait is shorter than 100 ns is not an error
+            eng.solve()
+    assert err.value.code == 5, str(err.value)     # GM_ERR_TIMEOUT
+    if eng is not None:
+        eng.delete()
+    ok = Engine.from_problem(P, threads=128, sync=True)
+    ok.solve()
+    assert rel(ok.get_solution(), want) < 1e-10
+    ok.delete()
