@@ -91,6 +91,7 @@ struct PolFP64 {
   __device__ static __forceinline__ AT zero() { return 0.0; }
   __device__ static __forceinline__ ST scalar(double s) { return s; }
   __device__ static __forceinline__ AT acc(AT a, VT v, double x) { return fma(v, x, a); }
+  __device__ static __forceinline__ AT norm(AT a) { return a; }
   __device__ static __forceinline__ AT mul(AT z, ST s) { return z * s; }
   __device__ static __forceinline__ AT add_mul(AT w, ST s, double v) { return fma(s, v, w); }
   __device__ static __forceinline__ AT sub_mul(AT w, ST s, double v) { return fma(-s, v, w); }
@@ -115,15 +116,23 @@ struct PolMixed {
   static constexpr bool kMixed = true;
   __device__ static __forceinline__ AT zero() { return {0.f, 0.f}; }
   __device__ static __forceinline__ ST scalar(double s) { return ff_from_double(s); }
-  __device__ static __forceinline__ AT acc(AT a, VT v, float x) { return ff_fma_ff(a, v, x); }
+  // SpMV row accumulation: hi gathers the exactly-split products (two_sum),
+  // lo collects every rounding error and stays unnormalised along the row;
+  // norm() renormalises once per row.  Over a row's few terms lo stays of
+  // order 2^-24 of the terms, so the sum keeps the float-float accuracy.
+  __device__ static __forceinline__ AT acc(AT a, VT v, float x) {
+    const ff p = two_prod(v, x);
+    const ff s = two_sum(a.hi, p.hi);
+    return {s.hi, a.lo + (s.lo + p.lo)};
+  }
   __device__ static __forceinline__ AT acc(AT a, VT v, float2 x) {
     // v * (x.hi + x.lo): exact v*x.hi plus the small v*x.lo term
-    ff p = two_prod(v, x.x);
-    p.lo = fmaf(v, x.y, p.lo);
-    ff s = two_sum(a.hi, p.hi);
-    float e = s.lo + (a.lo + p.lo);
-    return fast_two_sum(s.hi, e);
+    const ff p = two_prod(v, x.x);
+    const float pe = fmaf(v, x.y, p.lo);
+    const ff s = two_sum(a.hi, p.hi);
+    return {s.hi, a.lo + (s.lo + pe)};
   }
+  __device__ static __forceinline__ AT norm(AT a) { return fast_two_sum(a.hi, a.lo); }
   __device__ static __forceinline__ AT mul(AT z, ST s) { return ff_mul(z, s); }
   __device__ static __forceinline__ AT add_mul(AT w, ST s, float v) { return ff_add(w, ff_mulf(s, v)); }
   __device__ static __forceinline__ AT sub_mul(AT w, ST s, float v) { return ff_add(w, ff_neg(ff_mulf(s, v))); }

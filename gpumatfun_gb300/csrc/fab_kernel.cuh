@@ -361,6 +361,8 @@ __device__ __forceinline__ bool spmv_pass(const KParams& kp, const Ctx& c, ColSt
     const int* scol = cs.ready(kp, k, c.lane());
     AT z[R];
     spmv_slot<Pol, R, XT>(kp, s, c.lane(), x, z, scol);
+#pragma unroll
+    for (int r = 0; r < R; ++r) z[r] = Pol::norm(z[r]);
     epi(s, z);
     cs.release();
   }
