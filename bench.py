@@ -51,6 +51,9 @@ def parse():
                     help="mixed engine: 0 = diagonal-compensated FP32 matrix, 1 = plain FP32 values")
     ap.add_argument("--col-staging", type=int, default=0, choices=[0, 1],
                     help="0: stage SELL column indices in shared memory by TMA, 1: off")
+    ap.add_argument("--matrix-powers", type=int, default=None, choices=[0, 1],
+                    help="1: two Horner levels of the polynomial per SpMV pass "
+                         "(default: off for the f(A)b workloads, on for the adjoint)")
     ap.add_argument("--unfused", action="store_true",
                     help="step = build_subspace + lin_sys_solves + apply_V (three launches) instead of gm_solve")
     ap.add_argument("--l2-window", type=int, default=0, choices=[0, 1],
@@ -201,7 +204,8 @@ def run_ours(args, P, rank, world, local):
     R, K, W = args.nrhs, args.steps, args.warmup
     eng = Engine.from_problem(P, precision=args.precision, sync=False, l2_window=args.l2_window,
                               threads=args.threads, blocks_per_sm=args.bps,
-                              diag_compensation=args.diag_compensation, col_staging=args.col_staging)
+                              diag_compensation=args.diag_compensation, col_staging=args.col_staging,
+                              matrix_powers=args.matrix_powers or 0)
     eng.set_stream(stream.cuda_stream)
     n = P.n
     gen = torch.Generator(device=dev).manual_seed(1234 + rank)
@@ -300,6 +304,7 @@ def run_ours(args, P, rank, world, local):
             "config": config_of(args, P), "e2e": e2e, "gpu_launches": int(launches),
             "roofline": roof, "clocks": clocks,
             "engine": {"grid_blocks": info["grid_blocks"], "threads": info["threads"],
+                       "matrix_powers": info["matrix_powers"],
                        "sell_padded": info["sell_padded"], "device_bytes": info["device_bytes"]}}
     eng.delete()
     del B
@@ -392,7 +397,8 @@ def run_adjoint(args):
     out = {}
     ops = {}
     for prec in ("fp64", "mixed"):
-        ops[prec] = adjoint.FracFEOperator(mesh, kappa, precision=prec, **prm)
+        mp = 1 if args.matrix_powers is None else args.matrix_powers
+        ops[prec] = adjoint.FracFEOperator(mesh, kappa, precision=prec, matrix_powers=mp, **prm)
     setup_s = time.perf_counter() - t0
     op = ops["fp64"]
     dev = torch.device("cuda", 0)
@@ -469,7 +475,7 @@ def run_adjoint(args):
             "data": "synthetic (seeded disk mesh, two Gaussian-field coefficients kappa and kappa*, uniform b, "
                     "d = f(A(kappa*)) b + 1% noise)",
             "config": {"workload": args.workload, "n": int(op.n), "ntri": int(op.ntri), **prm,
-                       "l1": op.l1, "lN": op.lN},
+                       "l1": op.l1, "lN": op.lN, "matrix_powers": int(op.engine.info()["matrix_powers"])},
             "e2e": {"value": 1.0 / e2e_s, "unit": "grad-evals/s", "h2d_bytes_per_step": 8 * (2 * op.ntri + 3 * op.n),
                     "d2h_bytes_per_step": 8 * (op.ntri + 2 * op.n)},
             "fp64": out["fp64"], "mixed": out["mixed"],

@@ -114,14 +114,17 @@ class FracFEOperator:
 
     The contour (C nodes on [l1, lN]) and the polynomial preconditioner
     (degree ``degree`` on [0, lN]) are fixed at construction, so every kappa
-    evaluates the same approximation of f. [l1, lN] must enclose the
+    evaluates the same approximation of f.  ``matrix_powers`` runs two Horner
+    levels of the degree-``degree`` polynomial per SpMV pass (bit-identical
+    results; a few percent faster on meshes of a few 100k nodes). [l1, lN] must enclose the
     spectrum of every A(kappa) used. By default it is the spectrum of
     A(kappa0), widened by ``margin``.
     """
 
     def __init__(self, mesh: problems.FEMesh, kappa0: np.ndarray, alpha: float = 1.6, m: int = 150,
                  C: int = 32, degree: int = 16, l1: float | None = None, lN: float | None = None,
-                 margin: float = 2.0, precision: str = "fp64", store_basis: bool = True, **engine_kw):
+                 margin: float = 2.0, precision: str = "fp64", store_basis: bool = True,
+                 matrix_powers: int = 1, **engine_kw):
         self.st = fe_structure(mesh)
         self.alpha = float(alpha)
         self.f = params.frac_power(-alpha / 2)
@@ -143,7 +146,8 @@ class FracFEOperator:
         self.store_basis = bool(store_basis)
         self.engine = Engine(A0, np.zeros((n, R)), None, None, None, m, self.gamma, gs.real, gs.imag, [w] * R,
                              params.shifts_vector(sigma, m, R), col_scale=np.ones(R), precision=precision,
-                             sync=False, keep_entry_map=True, row_weight=self.st.msqrt, **engine_kw)
+                             sync=False, keep_entry_map=True, row_weight=self.st.msqrt,
+                             matrix_powers=matrix_powers, **engine_kw)
         self._fwd_key = None
         st = self.st
         self.engine.fe_attach(st.ntri, st.ent_ptr, st.ent_tri, st.ent_coef, st.tri_nodes, st.tri_kc)

@@ -8,6 +8,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -45,9 +46,9 @@ struct gm_engine {
   int scale_exp = 0;             // mixed engine: A stored as A * 2^-scale_exp
   unsigned long long epoch = 0;  // launch counter (progress-flag epochs)
   double dep_avg = 0.0;          // mean neighbour-list length per block
-  int Gk[5] = {};                // grid size per phase group (co-residency bound)
-  void* kfn[5] = {};
-  size_t smem[5] = {};           // dynamic shared memory per phase group
+  int Gk[7] = {};                // grid size per phase group (co-residency bound)
+  void* kfn[7] = {};
+  size_t smem[7] = {};           // dynamic shared memory per phase group
   std::vector<DevBuf> bufs;
   size_t bytes = 0;
   KParams kp{};
@@ -64,6 +65,9 @@ struct gm_engine {
   bool l2_window = false;        // launches carry an L2 persisting window over the matrix
   cudaAccessPolicyWindow window = {};
   bool keep_map = false;
+  bool mpk_req = false;          // matrix-powers passes requested
+  long long mpk_nmax = 0;        // largest own + halo rows of a block
+  std::vector<int> sell_col_host;  // SELL column indices kept for the halo build
   std::vector<double> roww;      // mixed engine: weights of the diagonal compensation (empty = ones)
   bool comp = false;             // mixed engine: diagonal compensation on
   int* row2slot = nullptr;       // device, kept with the entry map: row -> 32 * slice + lane
@@ -313,6 +317,7 @@ int upload_sell(gm_engine* e, const Csr& A, int sigma, int scale_exp, const std:
   long long* d_off;
   int rc;
   if ((rc = dupload(e, &d_off, off.data(), off.size()))) return rc;
+  if (e->mpk_req && np == 1 && !(sorted || np > 1)) e->sell_col_host = col;
   // Diagonal compensation of the FP32-stored matrix: row r gets the extra
   // diagonal term c_r = sum_t (a_t 2^-e - fl32(a_t 2^-e)) w_col(t) / w_r, so
   // that the stored operator maps w exactly as A does.  The small eigenvalues
@@ -408,7 +413,7 @@ int build_partition(gm_engine* e, const Csr& A, const std::vector<long long>& ro
   for (int p = 0; p < np; ++p) pb0[p + 1] = pb0[p] + gp[p];
   const int G = pb0[np];
   e->G = G;
-  for (int g = 0; g < 5; ++g) e->Gk[g] = G;
+  for (int g = 0; g < 7; ++g) e->Gk[g] = G;   // every phase group
   e->kp.G = G;
   std::vector<int> bs(G + 1, 0), bprob(G, 0);
   for (int p = 0; p < np; ++p) {
@@ -448,6 +453,59 @@ int build_partition(gm_engine* e, const Csr& A, const std::vector<long long>& ro
           }
         }
       }
+  // Matrix-powers passes: per block the halo rows (referenced by its rows,
+  // owned elsewhere), local column indices, and waits over two hops.
+  const bool mpk = e->mpk_req && !e->sell_col_host.empty();
+  std::vector<long long> hptr;
+  std::vector<int> hrows, lcol;
+  if (mpk) {
+    hptr.assign(G + 1, 0);
+    lcol.assign(e->sell_col_host.size(), 0);
+    std::vector<unsigned char> adj2 = adj;
+    long long nmax = 0;
+    for (int q = 0; q < G; ++q) {
+      const long long rb0 = (long long)bs[q] * 32;
+      const long long rb1 = std::min<long long>((long long)bs[q + 1] * 32, e->n);
+      std::vector<int> halo;
+      for (long long r = rb0; r < rb1; ++r)
+        for (long long t = A.ptr[r]; t < A.ptr[r + 1]; ++t) {
+          const int col = A.col[t];
+          if (col < rb0 || col >= rb1) halo.push_back(col);
+        }
+      std::sort(halo.begin(), halo.end());
+      halo.erase(std::unique(halo.begin(), halo.end()), halo.end());
+      const long long nown = rb1 - rb0;
+      nmax = std::max<long long>(nmax, nown + (long long)halo.size());
+      // two hops: the owners of the halo rows' columns
+      for (int hr : halo)
+        for (long long t = A.ptr[hr]; t < A.ptr[hr + 1]; ++t) {
+          const int o = owner[A.col[t]];
+          if (o != q) {
+            adj2[(size_t)q * G + o] = 1;
+            adj2[(size_t)o * G + q] = 1;
+          }
+        }
+      // local column index of every slot of the block's slices
+      for (long long sl = bs[q]; sl < bs[q + 1]; ++sl)
+        for (long long slot = off[sl]; slot < off[sl + 1]; ++slot) {
+          const int col = e->sell_col_host[slot];
+          int li = 0;
+          if (col >= rb0 && col < rb1) {
+            li = (int)(col - rb0);
+          } else {
+            const auto it = std::lower_bound(halo.begin(), halo.end(), col);
+            if (it != halo.end() && *it == col) li = (int)(nown + (it - halo.begin()));
+          }
+          lcol[slot] = li;
+        }
+      hrows.insert(hrows.end(), halo.begin(), halo.end());
+      hptr[q + 1] = (long long)hrows.size();
+    }
+    adj.swap(adj2);
+    e->mpk_nmax = nmax;
+  }
+  e->sell_col_host.clear();
+  e->sell_col_host.shrink_to_fit();
   std::vector<int> dp(G + 1, 0), di;
   for (int q = 0; q < G; ++q) {
     for (int o = 0; o < G; ++o)
@@ -479,12 +537,43 @@ int build_partition(gm_engine* e, const Csr& A, const std::vector<long long>& ro
   e->kp.dep_ptr = d_dp;
   e->kp.dep_idx = d_di;
   e->kp.prog = d_prog;
+  e->kp.mpk = 0;
+  if (mpk) {
+    long long* d_hptr;
+    int* d_hrows;
+    int* d_lcol;
+    if ((rc = dupload(e, &d_hptr, hptr.data(), hptr.size()))) return rc;
+    if (hrows.empty()) hrows.push_back(0);
+    if ((rc = dupload(e, &d_hrows, hrows.data(), hrows.size()))) return rc;
+    if ((rc = dupload(e, &d_lcol, lcol.data(), lcol.size()))) return rc;
+    e->kp.halo_ptr = d_hptr;
+    e->kp.halo_rows = d_hrows;
+    e->kp.lcol = d_lcol;
+    e->kp.mpk = 1;   // confirmed (or withdrawn) once the shared memory is sized
+  }
   return GM_OK;
 }
 
 // Phase-group kernels (kern_fp64.cu / kern_mixed.cu): 0 lanczos, 1 solves,
 // 2 apply, 3 deflate/update, 4 fused lanczos + solves + apply.
-enum { KGRP_LANCZOS = 0, KGRP_SOLVE = 1, KGRP_APPLY = 2, KGRP_DEFLATE = 3, KGRP_FUSED = 4, KGRP_N = 5 };
+enum { KGRP_LANCZOS = 0, KGRP_SOLVE = 1, KGRP_APPLY = 2, KGRP_DEFLATE = 3, KGRP_FUSED = 4,
+       KGRP_LANCZOS_MPK = 5, KGRP_FUSED_MPK = 6, KGRP_N = 7 };
+
+// The dynamic shared memory limit is an attribute of the kernel function,
+// shared by every handle of the process (per device): only ever raise it, so
+// that a handle created later with less shared memory cannot lower the limit
+// under an earlier one.
+cudaError_t raise_smem_limit(int dev, void* kfn, size_t bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, void*>, size_t> set;
+  if (bytes <= 48 * 1024) return cudaSuccess;
+  std::lock_guard<std::mutex> lock(mu);
+  size_t& cur = set[{dev, kfn}];
+  if (bytes <= cur) return cudaSuccess;
+  const cudaError_t st = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  if (st == cudaSuccess) cur = bytes;
+  return st;
+}
 
 void* pick_kernel(int prec, int R, int group) {
   return prec == GM_FP64 ? gm::kernel_fp64(R, group) : gm::kernel_mixed(R, group);
@@ -525,7 +614,9 @@ int launch(gm_engine* e, int phases, int slot) {
   KParams kp = e->kp;
   kp.phases = phases;
   void* args[] = {&kp};
-  const int grp = group_of(phases);
+  int grp = group_of(phases);
+  if (e->kp.mpk && (grp == KGRP_LANCZOS || grp == KGRP_FUSED))
+    grp = grp == KGRP_LANCZOS ? KGRP_LANCZOS_MPK : KGRP_FUSED_MPK;
   kp.G = e->Gk[grp];
   if (e->capturing) {
     // A captured launch replays with the same parameters, so the progress
@@ -640,6 +731,7 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
 
   e->keep_map = a->keep_entry_map != 0 && np == 1;
   e->comp = a->precision == GM_MIXED && a->diag_compensation == 0;
+  e->mpk_req = a->matrix_powers != 0 && np == 1 && a->sell_sigma <= 1 && a->gamma_size >= 3;
   if (e->comp && a->row_weight) {
     if (np != 1) return fail(e, GM_ERR_ARG, "row_weight applies to a single problem");
     e->roww.assign(a->row_weight, a->row_weight + probs[0].n);
@@ -710,9 +802,10 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
   for (int g = 0; g < KGRP_N; ++g) {
     e->kfn[g] = pick_kernel(e->prec, e->R, g);
     if (!e->kfn[g]) return fail(e, GM_ERR_UNSUPPORTED, "no kernel for nrhs %d", e->R);
-    e->smem[g] = (g == KGRP_LANCZOS || g == KGRP_APPLY || g == KGRP_FUSED) ? stage_smem : 0;
+    e->smem[g] = (g == KGRP_LANCZOS || g == KGRP_APPLY || g == KGRP_FUSED || g == KGRP_LANCZOS_MPK ||
+                  g == KGRP_FUSED_MPK) ? stage_smem : 0;
     if (e->smem[g] > 48 * 1024)
-      GM_CUDA(e, cudaFuncSetAttribute(e->kfn[g], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)e->smem[g]));
+      GM_CUDA(e, raise_smem_limit(e->dev, e->kfn[g], e->smem[g]));
     int nb = 0;
     GM_CUDA(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, e->kfn[g], e->threads, e->smem[g]));
     if (nb < 1) return fail(e, GM_ERR_UNSUPPORTED, "kernel group %d cannot be resident with %d threads", g, e->threads);
@@ -726,6 +819,31 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
   // blocks per problem and the slice partition (sets e->G to the blocks used)
   if ((rc = build_partition(e, csr, slot_rows, slice_off, pslice0, prow0))) return rc;
   e->kp.dep_mode = a->sync_policy == 0 ? 1 : 0;
+  if (e->kp.mpk) {
+    // the level in between lives in dynamic shared memory after the stages;
+    // keep it only if the Lanczos kernels stay as resident as the grid needs
+    const size_t su_off = (e->smem[KGRP_LANCZOS] + 15) & ~(size_t)15;
+    const size_t su_bytes = (size_t)e->mpk_nmax * e->R * 8;
+    const int need = (e->G + e->nsm - 1) / e->nsm;
+    bool fits = true;
+    for (int g : {KGRP_LANCZOS_MPK, KGRP_FUSED_MPK}) {
+      const size_t sm = su_off + su_bytes;
+      if (raise_smem_limit(e->dev, e->kfn[g], sm) != cudaSuccess) {
+        cudaGetLastError();
+        fits = false;
+        break;
+      }
+      int nb = 0;
+      GM_CUDA(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, e->kfn[g], e->threads, sm));
+      if (nb < need) { fits = false; break; }
+    }
+    if (fits) {
+      e->smem[KGRP_LANCZOS_MPK] = e->smem[KGRP_FUSED_MPK] = su_off + su_bytes;
+      e->kp.su_off = (long long)su_off;
+    } else {
+      e->kp.mpk = 0;   // the two-hop waits stay: correct, slightly more waiting
+    }
+  }
   csr = Csr();
   if (a->l2_window == 0 && e->mat_bytes > 0) {
     // Persisting L2 lines for the matrix, which every SpMV pass re-reads: the
@@ -1442,6 +1560,7 @@ int gm_info(gm_handle h, int64_t* info) {
   info[6] = h->prec; info[7] = h->G; info[8] = h->threads; info[9] = h->padded;
   info[10] = (int64_t)h->bytes; info[11] = h->launches;
   info[12] = h->nprob;
+  info[13] = h->kp.mpk;
   return GM_OK;
 }
 

@@ -27,7 +27,8 @@ namespace gm {
 enum Phase : int {
   PH_LANCZOS = 1, PH_TRISOLVE = 2, PH_COEF = 4, PH_APPLY = 8,
   PH_UPDATE_FKPP = 16, PH_UPDATE_FHN = 32, PH_DEFLATE = 64,
-  PH_APPLY_SET = 128   // apply writes X = lift (fused solve) instead of X += lift
+  PH_APPLY_SET = 128,  // apply writes X = lift (fused solve) instead of X += lift
+  PH_MPK = 256         // compile-time only: entry points with matrix-powers Horner passes
 };
 
 struct KParams {
@@ -82,6 +83,15 @@ struct KParams {
   const int* prob_blk0;       // [nprob+1] first block of each problem
   const long long* prob_row0; // [nprob+1] first row of each problem
   int stage_cap;              // >0: stage each slice's column indices in shared memory by TMA
+  // Two Horner levels per pass (matrix powers): per block, the rows its rows
+  // reference outside its own range (halo), the SELL column indices in block-
+  // local numbering (own rows first, then the halo), and the offset of the
+  // local vector in dynamic shared memory.  Enabled only without a row perm.
+  int mpk;
+  long long su_off;
+  const long long* halo_ptr;  // [G + 1]
+  const int* halo_rows;
+  const int* lcol;            // per SELL slot
                               // bulk copies (slices of at most stage_cap columns); 0: off
   int* status;
   int* meff;        // [R]
@@ -199,12 +209,13 @@ struct ChunkWidth {
 
 template <class Pol, int R, class XT>
 __device__ __forceinline__ void spmv_slot(const KParams& kp, long long s, int lane, const XT* __restrict__ x,
-                                          typename Pol::AT (&acc)[R], const int* scol = nullptr) {
+                                          typename Pol::AT (&acc)[R], const int* scol = nullptr,
+                                          const int* colarr = nullptr) {
   using VT = typename Pol::VT;
   constexpr int CH = ChunkWidth<VT, XT, R>::value;
   const long long base = kp.slice_off[s];
   const int len = (int)((kp.slice_off[s + 1] - base) >> 5);
-  const int* cp = kp.col + base + lane;
+  const int* cp = (colarr ? colarr : kp.col) + base + lane;
   const VT* vp = reinterpret_cast<const VT*>(kp.val) + base + lane;
 #pragma unroll
   for (int r = 0; r < R; ++r) acc[r] = Pol::zero();
@@ -369,6 +380,105 @@ __device__ __forceinline__ bool spmv_pass(const KParams& kp, const Ctx& c, ColSt
   return true;
 }
 
+// One row of A x read through the SELL layout without a row perm (row r is
+// lane r % 32 of slice r / 32): the halo rows of a matrix-powers pass.
+template <class Pol, int R, class XT>
+__device__ __forceinline__ void row_spmv(const KParams& kp, long long r, const XT* __restrict__ x,
+                                         typename Pol::AT (&acc)[R]) {
+  using VT = typename Pol::VT;
+  const long long s = r >> 5;
+  const int l = (int)(r & 31);
+  const long long base = kp.slice_off[s];
+  const int len = (int)((kp.slice_off[s + 1] - base) >> 5);
+  const VT* vp = reinterpret_cast<const VT*>(kp.val) + base + l;
+  const int* cp = kp.col + base + l;
+#pragma unroll
+  for (int q = 0; q < R; ++q) acc[q] = Pol::zero();
+  float dl = 0.f;
+  if constexpr (Pol::kMixed) {
+    if (kp.dlo) dl = __ldg(kp.dlo + s * 32 + l);
+  }
+  for (int jj = 0; jj < len; ++jj) {
+    const int cc = __ldg(cp + (long long)jj * 32);
+    const VT a = __ldg(vp + (long long)jj * 32);
+    XT xv[R];
+    VecIO<R>::ld(x + (long long)cc * R, xv);
+    if constexpr (Pol::kMixed) {
+      if (jj == 0) {
+#pragma unroll
+        for (int q = 0; q < R; ++q) acc[q] = Pol::acc(acc[q], dl, xv[q]);
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < R; ++q) acc[q] = Pol::acc(acc[q], a, xv[q]);
+  }
+#pragma unroll
+  for (int q = 0; q < R; ++q) acc[q] = Pol::norm(acc[q]);
+}
+
+// Two Horner levels in one pass (matrix powers):
+//   level 1  u1 = A hin + g1 w   on the block's rows and its halo rows,
+//            kept in shared memory in block-local numbering;
+//   level 2  hout = A u1 + g2 w  on the block's rows, A read with local
+//            column indices against the shared-memory vector.
+// The ordering wait before it covers two hops of the row graph (the halo
+// rows' neighbours), as every wait does when these passes are enabled.
+template <class Pol, int R>
+__device__ __forceinline__ bool horner_pair(const KParams& kp, const Ctx& c, ColStage& cs, PassSync& ps,
+                            const typename Pol::HT* hin, typename Pol::HT* hout, const typename Pol::BT* w,
+                            const typename Pol::ST (&g1)[R], const typename Pol::ST (&g2)[R]) {
+  using BT = typename Pol::BT;
+  using HT = typename Pol::HT;
+  using AT = typename Pol::AT;
+  extern __shared__ __align__(128) unsigned char dsm[];
+  HT* const su = reinterpret_cast<HT*>(dsm + kp.su_off);
+  const long long sb = kp.blk_slice[c.b()], se = kp.blk_slice[c.b() + 1];
+  const long long rb0 = sb * 32;
+  const long long nown = (se * 32 < kp.n ? se * 32 : kp.n) - rb0;
+  // level 1, own rows (the usual pass, results to shared memory)
+  const bool ok = spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
+    const long long row = s * 32 + c.lane();
+    if (row >= kp.n) return;
+    BT sv[R];
+    VecIO<R>::ld(w + row * R, sv);
+    HT u[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) u[r] = Pol::to_h(Pol::add_mul(z[r], g1[r], sv[r]));
+    VecIO<R>::st(su + (row - rb0) * R, u);
+  }, &ps);
+  if (!ok) return false;
+  // level 1, halo rows
+  const long long h0 = kp.halo_ptr[c.b()], h1 = kp.halo_ptr[c.b() + 1];
+  for (long long k = h0 + c.tid(); k < h1; k += c.nt()) {
+    const long long r = kp.halo_rows[k];
+    AT z[R];
+    row_spmv<Pol, R, HT>(kp, r, hin, z);
+    BT sv[R];
+    VecIO<R>::ld(w + r * R, sv);
+    HT u[R];
+#pragma unroll
+    for (int q = 0; q < R; ++q) u[q] = Pol::to_h(Pol::add_mul(z[q], g1[q], sv[q]));
+    VecIO<R>::st(su + (nown + (k - h0)) * R, u);
+  }
+  __syncthreads();
+  // level 2, own rows from the shared-memory vector
+  for (long long s = sb + c.warp(); s < se; s += c.nw()) {
+    AT z[R];
+    spmv_slot<Pol, R, HT>(kp, s, c.lane(), su, z, nullptr, kp.lcol);
+#pragma unroll
+    for (int r = 0; r < R; ++r) z[r] = Pol::norm(z[r]);
+    const long long row = s * 32 + c.lane();
+    if (row >= kp.n) continue;
+    BT sv[R];
+    VecIO<R>::ld(w + row * R, sv);
+    HT u[R];
+#pragma unroll
+    for (int r = 0; r < R; ++r) u[r] = Pol::to_h(Pol::add_mul(z[r], g2[r], sv[r]));
+    VecIO<R>::st(hout + row * R, u);
+  }
+  return true;
+}
+
 // ------------------------------------------------------------------ LANCZOS
 // build_subspace.cu:5-89 with the three-term recurrence as two grid passes
 // per step (A: SpMV + beta_j v_{j-1} + alpha partials; B: w -= alpha v_j +
@@ -407,7 +517,7 @@ __device__ __forceinline__ void grid_total_smem(const double* partials, int stri
   __syncthreads();
 }
 
-template <class Pol, int R>
+template <class Pol, int R, bool MPK>
 __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, PassSync& ps, ColStage& cs) {
   using BT = typename Pol::BT;
   using HT = typename Pol::HT;
@@ -472,7 +582,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
     // not read, in the accumulator precision; pass B subtracts alpha_j v_j and
     // rounds once to storage (rounding before the subtraction would make the
     // storage error relative to |w| instead of to beta_{j+1} << |w|).
-    HT* const Hw = (d & 1) ? H0 : H1;
+    HT* Hw = (d & 1) ? H0 : H1;
     if (c.tid() == 0) {
       for (int r = 0; r < R; ++r) {
         sh.sc[r] = Pol::scalar(sh.rbeta[r] * gam[0]);
@@ -526,24 +636,56 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
         });
       }
       ps.done(kp);
-      for (int h = 2; h <= d; ++h) {
-        const HT* hin = (h & 1) ? H0 : H1;
-        HT* hout = (h & 1) ? H1 : H0;
-        const bool ok = spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
-          const long long row = slot_row(kp, s, c.lane());
-          if (row < 0) return;
-          BT sv[R];
-          VecIO<R>::ld(src + row * R, sv);
-          HT u[R];
+      const HT* hin;
+      if constexpr (MPK) {
+        // Horner levels 2..d, pairs in one pass each, then single passes;
+        // hcur holds the latest level, the other buffer takes the next
+        HT* hcur = H1;
+        HT* hnxt = H0;
+        int h = 2;
+        for (; h + 1 <= d; h += 2) {
+          if (!horner_pair<Pol, R>(kp, c, cs, ps, hcur, hnxt, src, sh.gr[h], sh.gr[h + 1])) return false;
+          ps.done(kp);
+          HT* t = hcur; hcur = hnxt; hnxt = t;
+        }
+        for (; h <= d; ++h) {
+          HT* hout = hnxt;
+          const bool ok = spmv_pass<Pol, R, HT>(kp, c, cs, hcur, [&](long long s, AT (&z)[R]) {
+            const long long row = slot_row(kp, s, c.lane());
+            if (row < 0) return;
+            BT sv[R];
+            VecIO<R>::ld(src + row * R, sv);
+            HT u[R];
 #pragma unroll
-          for (int r = 0; r < R; ++r) u[r] = Pol::to_h(Pol::add_mul(z[r], sh.gr[h][r], sv[r]));
-          VecIO<R>::st(hout + row * R, u);
-        }, &ps);
-        if (!ok) return false;
-        ps.done(kp);
+            for (int r = 0; r < R; ++r) u[r] = Pol::to_h(Pol::add_mul(z[r], sh.gr[h][r], sv[r]));
+            VecIO<R>::st(hout + row * R, u);
+          }, &ps);
+          if (!ok) return false;
+          ps.done(kp);
+          HT* t = hcur; hcur = hnxt; hnxt = t;
+        }
+        hin = hcur;
+        Hw = hnxt;   // w goes to the buffer the final pass does not read
+      } else {
+        for (int h = 2; h <= d; ++h) {
+          const HT* hin_h = (h & 1) ? H0 : H1;
+          HT* hout = (h & 1) ? H1 : H0;
+          const bool ok = spmv_pass<Pol, R, HT>(kp, c, cs, hin_h, [&](long long s, AT (&z)[R]) {
+            const long long row = slot_row(kp, s, c.lane());
+            if (row < 0) return;
+            BT sv[R];
+            VecIO<R>::ld(src + row * R, sv);
+            HT u[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) u[r] = Pol::to_h(Pol::add_mul(z[r], sh.gr[h][r], sv[r]));
+            VecIO<R>::st(hout + row * R, u);
+          }, &ps);
+          if (!ok) return false;
+          ps.done(kp);
+        }
+        hin = (d & 1) ? H1 : H0;
       }
       // final pass: w = A u - beta_j v_{j-1}
-      const HT* hin = (d & 1) ? H1 : H0;
       const bool ok = spmv_pass<Pol, R, HT>(kp, c, cs, hin, [&](long long s, AT (&z)[R]) {
         const long long row = slot_row(kp, s, c.lane());
         if (row < 0) return;
@@ -976,7 +1118,7 @@ __global__ void __launch_bounds__(GM_MAXT, (R >= 4 ? 1 : GM_MINB)) fab_kernel(KP
   };
   if ((PH & PH_LANCZOS) && (ph & PH_LANCZOS)) {
     if (!sep()) return;
-    if (!phase_lanczos<Pol, R>(kp, c, g, ps, cs)) return;
+    if (!phase_lanczos<Pol, R, (PH & PH_MPK) != 0>(kp, c, g, ps, cs)) return;
   }
   if ((PH & PH_TRISOLVE) && (ph & PH_TRISOLVE)) {
     if (!sep()) return;

@@ -10,6 +10,8 @@ static void* group_ptr(int group) {
     case 2: return (void*)fab_kernel<Pol, R, KG_APPLY>;
     case 3: return (void*)fab_kernel<Pol, R, KG_DEFLATE>;
     case 4: return (void*)fab_kernel<Pol, R, KG_LANCZOS | KG_SOLVE | KG_APPLY>;
+    case 5: return (void*)fab_kernel<Pol, R, KG_LANCZOS | PH_MPK>;
+    case 6: return (void*)fab_kernel<Pol, R, KG_LANCZOS | KG_SOLVE | KG_APPLY | PH_MPK>;
   }
   return nullptr;
 }

@@ -121,6 +121,11 @@ typedef struct gm_create_args {
                                   near-null vector: ones for a graph Laplacian,
                                   M^{1/2} 1 for M^{-1/2} K M^{-1/2}); NULL = ones  */
   int diag_compensation;       /* mixed engine: 0 = on (default), 1 = off          */
+  int matrix_powers;           /* 1 = two Horner levels of the polynomial per SpMV
+                                  pass (halo rows recomputed per block, the level
+                                  in between in shared memory), where it applies:
+                                  one problem, no sigma sorting, the vector fits
+                                  shared memory; 0 = one level per pass            */
 } gm_create_args;
 
 /* Fill *args with defaults (zeros, struct_version, sync_mode = 1, nrhs = 2). */
@@ -298,8 +303,9 @@ int gm_phase_times(gm_handle h, float* ms5);
 
 /* Engine facts: [0] n, [1] nrhs, [2] m, [3] d, [4] C, [5] k, [6] precision,
  * [7] grid blocks, [8] threads per block, [9] SELL padded entries,
- * [10] device bytes held, [11] kernel launches so far, [12] problems. */
-int gm_info(gm_handle h, int64_t* info13);
+ * [10] device bytes held, [11] kernel launches so far, [12] problems,
+ * [13] 1 when matrix-powers passes are active.  info has 14 entries. */
+int gm_info(gm_handle h, int64_t* info14);
 
 /* Effective Krylov dimension per (problem, RHS) after the last build (< m
  * after a breakdown). */

@@ -144,3 +144,35 @@ def test_wait_limit_reports_timeout_and_context_survives(engine_lib):
     ok.solve()
     assert rel(ok.get_solution(), want) < 1e-10
     ok.delete()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("R,degree", [(1, 8), (2, 5), (1, 3), (4, 6)])
+def test_matrix_powers_passes_are_bit_identical(engine_lib, precision, R, degree):
+    """Two Horner levels per pass (halo rows recomputed per block, the level
+    in between in shared memory) run the same operations in the same order as
+    one level per pass: the results agree bit for bit, on a grid of hundreds
+    of blocks whose two-hop waits are exercised."""
+    from gpumatfun_gb300 import adjoint
+    mesh = __import__("gpumatfun_gb300").problems.disk_mesh(40000, seed=2)
+    cent = mesh.nodes[mesh.tris].mean(axis=1)
+    kappa = np.exp(__import__("gpumatfun_gb300").problems.gaussian_random_field(cent, sigma=1.0, ell=0.1, seed=3))
+    A = adjoint.fe_structure(mesh).matrix(kappa)
+    lam_hi = 1.05 * float(__import__("scipy.sparse.linalg", fromlist=["eigsh"]).eigsh(
+        A, k=1, which="LA", return_eigenvectors=False, tol=1e-4)[0])
+    f = params.frac_power(-0.8)
+    rng = np.random.default_rng(R + degree)
+    U = rng.random((A.shape[0], R))
+    P = workloads.make_problem("mpk", A, U, np.zeros((A.shape[0], 0)), np.zeros(0), [f] * R, 12, 16,
+                               lam_hi / 2e4, lam_hi, degree=degree, prob_dim=lam_hi / 4)
+    out = []
+    for mp in (0, 1):
+        eng = Engine.from_problem(P, precision=precision, threads=128, sync=False, matrix_powers=mp)
+        assert eng.info()["grid_blocks"] > 200
+        assert eng.info()["matrix_powers"] == mp
+        eng.solve()
+        out.append(eng.get_solution())
+        eng.delete()
+    np.testing.assert_array_equal(out[0], out[1])
+    if precision == "fp64" and R <= 2:
+        assert rel(out[1], oracle(P)) < 1e-10
