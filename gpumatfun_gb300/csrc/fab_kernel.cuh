@@ -461,10 +461,35 @@ __device__ __forceinline__ bool horner_pair(const KParams& kp, const Ctx& c, Col
     VecIO<R>::st(su + (nown + (k - h0)) * R, u);
   }
   __syncthreads();
-  // level 2, own rows from the shared-memory vector
+  // level 2, own rows from the shared-memory vector: its gathers have
+  // shared-memory latency, so one entry at a time (few live registers)
+  using VT = typename Pol::VT;
   for (long long s = sb + c.warp(); s < se; s += c.nw()) {
+    const long long base = kp.slice_off[s];
+    const int len = (int)((kp.slice_off[s + 1] - base) >> 5);
+    const int* lp = kp.lcol + base + c.lane();
+    const VT* vp = reinterpret_cast<const VT*>(kp.val) + base + c.lane();
     AT z[R];
-    spmv_slot<Pol, R, HT>(kp, s, c.lane(), su, z, nullptr, kp.lcol);
+#pragma unroll
+    for (int r = 0; r < R; ++r) z[r] = Pol::zero();
+    float dl = 0.f;
+    if constexpr (Pol::kMixed) {
+      if (kp.dlo) dl = __ldg(kp.dlo + s * 32 + c.lane());
+    }
+    for (int jj = 0; jj < len; ++jj) {
+      const int lc = __ldg(lp + (long long)jj * 32);
+      const VT a = __ldg(vp + (long long)jj * 32);
+      HT xv[R];
+      VecIO<R>::ld(su + (long long)lc * R, xv);
+      if constexpr (Pol::kMixed) {
+        if (jj == 0) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) z[r] = Pol::acc(z[r], dl, xv[r]);
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < R; ++r) z[r] = Pol::acc(z[r], a, xv[r]);
+    }
 #pragma unroll
     for (int r = 0; r < R; ++r) z[r] = Pol::norm(z[r]);
     const long long row = s * 32 + c.lane();
