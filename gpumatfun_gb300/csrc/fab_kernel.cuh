@@ -663,19 +663,19 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
       ps.done(kp);
       const HT* hin;
       if constexpr (MPK) {
-        // Horner levels 2..d, pairs in one pass each, then single passes;
-        // hcur holds the latest level, the other buffer takes the next
-        HT* hcur = H1;
-        HT* hnxt = H0;
-        int h = 2;
-        for (; h + 1 <= d; h += 2) {
-          if (!horner_pair<Pol, R>(kp, c, cs, ps, hcur, hnxt, src, sh.gr[h], sh.gr[h + 1])) return false;
+        // Horner levels 2..d, pairs in one pass each, then single passes.
+        // Pass k (0-based, after pass 1) reads H1 when k is even, H0 when odd,
+        // and writes the other buffer.
+        int k = 0, h = 2;
+        for (; h + 1 <= d; h += 2, ++k) {
+          if (!horner_pair<Pol, R>(kp, c, cs, ps, (k & 1) ? H0 : H1, (k & 1) ? H1 : H0, src, sh.gr[h],
+                                   sh.gr[h + 1]))
+            return false;
           ps.done(kp);
-          HT* t = hcur; hcur = hnxt; hnxt = t;
         }
-        for (; h <= d; ++h) {
-          HT* hout = hnxt;
-          const bool ok = spmv_pass<Pol, R, HT>(kp, c, cs, hcur, [&](long long s, AT (&z)[R]) {
+        for (; h <= d; ++h, ++k) {
+          HT* hout = (k & 1) ? H1 : H0;
+          const bool ok = spmv_pass<Pol, R, HT>(kp, c, cs, (k & 1) ? H0 : H1, [&](long long s, AT (&z)[R]) {
             const long long row = slot_row(kp, s, c.lane());
             if (row < 0) return;
             BT sv[R];
@@ -687,10 +687,9 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
           }, &ps);
           if (!ok) return false;
           ps.done(kp);
-          HT* t = hcur; hcur = hnxt; hnxt = t;
         }
-        hin = hcur;
-        Hw = hnxt;   // w goes to the buffer the final pass does not read
+        hin = (k & 1) ? H0 : H1;
+        Hw = (k & 1) ? H1 : H0;   // w goes to the buffer the final pass does not read
       } else {
         for (int h = 2; h <= d; ++h) {
           const HT* hin_h = (h & 1) ? H0 : H1;
