@@ -5,7 +5,8 @@ keeps the fastest.  The knobs are the ones the engine exposes at create time:
 - threads per block (the row-block size: 32 SELL rows per warp);
 - resident blocks per SM;
 - TMA staging of SELL column indices on or off;
-- neighbour waits vs grid barriers between SpMV passes.
+- neighbour waits vs grid barriers between SpMV passes;
+- one or two Horner levels of the polynomial per SpMV pass (degree >= 2).
 
 Results are cached in a JSON file keyed by a signature of the workload:
 - n, nnz, a row-length histogram and the number of right-hand sides;
@@ -42,13 +43,17 @@ def signature(P, precision: str, device: str = "") -> str:
     return hashlib.sha1(json.dumps(key, sort_keys=True).encode()).hexdigest()[:16]
 
 
-def candidates(R: int) -> list:
-    """The search space (row-block sizes, residency, staging, pass ordering)."""
+def candidates(R: int, degree: int = 0) -> list:
+    """The search space: row-block sizes, residency, staging, pass ordering
+    and, for a polynomial of degree >= 2, matrix-powers passes (neighbour
+    waits only)."""
     threads = (128, 256, 512)
     bps = (0, 1) if R >= 4 else (0, 1, 2)
     out = []
     for t, b, stg, pol in itertools.product(threads, bps, (0, 1), (0, 1)):
-        out.append(dict(threads=t, blocks_per_sm=b, col_staging=stg, sync_policy=pol))
+        out.append(dict(threads=t, blocks_per_sm=b, col_staging=stg, sync_policy=pol, matrix_powers=0))
+        if degree >= 2 and pol == 0:
+            out.append(dict(threads=t, blocks_per_sm=b, col_staging=stg, sync_policy=pol, matrix_powers=1))
     return out
 
 
@@ -92,7 +97,7 @@ def tune(P, precision: str = "fp64", reps: int = 3, cache_path: str | None = Non
         return dict(cache[key], cached=True)
     measure = measure or _measure_engine(P, precision, reps)
     best, best_ms, trials = None, float("inf"), []
-    for cand in (space or candidates(P.R)):
+    for cand in (space or candidates(P.R, P.d)):
         ms = measure(cand)
         trials.append(dict(cand, ms=ms))
         if ms < best_ms:

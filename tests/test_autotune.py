@@ -28,3 +28,9 @@ def test_tune_picks_fastest_and_caches(tmp_path):
 def test_candidates_respect_rhs():
     assert all(c["blocks_per_sm"] in (0, 1) for c in autotune.candidates(4))
     assert {c["threads"] for c in autotune.candidates(1)} == {128, 256, 512}
+
+
+def test_matrix_powers_candidates_only_with_a_polynomial():
+    assert all(c["matrix_powers"] == 0 for c in autotune.candidates(1, 0))
+    mp = [c for c in autotune.candidates(1, 8) if c["matrix_powers"] == 1]
+    assert mp and all(c["sync_policy"] == 0 for c in mp)
