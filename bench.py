@@ -47,6 +47,7 @@ def parse():
     ap.add_argument("--cpu-sample-s", type=float, default=30.0)
     ap.add_argument("--threads", type=int, default=0, help="threads per block (0: engine default)")
     ap.add_argument("--bps", type=int, default=0, help="resident blocks per SM (0: engine default)")
+    ap.add_argument("--max-blocks", type=int, default=0, help="cap on the grid size (0: engine default)")
     ap.add_argument("--diag-compensation", type=int, default=0, choices=[0, 1],
                     help="mixed engine: 0 = diagonal-compensated FP32 matrix, 1 = plain FP32 values")
     ap.add_argument("--col-staging", type=int, default=0, choices=[0, 1],
@@ -205,7 +206,7 @@ def run_ours(args, P, rank, world, local):
     eng = Engine.from_problem(P, precision=args.precision, sync=False, l2_window=args.l2_window,
                               threads=args.threads, blocks_per_sm=args.bps,
                               diag_compensation=args.diag_compensation, col_staging=args.col_staging,
-                              matrix_powers=args.matrix_powers or 0)
+                              matrix_powers=args.matrix_powers or 0, max_blocks=args.max_blocks)
     eng.set_stream(stream.cuda_stream)
     n = P.n
     gen = torch.Generator(device=dev).manual_seed(1234 + rank)

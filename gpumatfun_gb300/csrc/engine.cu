@@ -812,6 +812,7 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
     const int bps = a->blocks_per_sm > 0 ? std::min(a->blocks_per_sm, nb) : nb;
     long long G = (long long)bps * e->nsm;
     if (a->blocks_per_sm <= 0) G = std::min(G, want);
+    if (a->max_blocks > 0) G = std::min<long long>(G, std::max<long long>(np, a->max_blocks));
     e->Gk[g] = (int)std::max<long long>(1, G);
     Gmax = Gmax == 0 ? e->Gk[g] : std::min(Gmax, (long long)e->Gk[g]);
   }

@@ -63,7 +63,7 @@ class CreateArgs(ct.Structure):
         ("sync_policy", ct.c_int), ("col_staging", ct.c_int), ("keep_entry_map", ct.c_int),
         ("l2_window", ct.c_int),
         ("row_weight", _dp), ("diag_compensation", ct.c_int),
-        ("matrix_powers", ct.c_int),
+        ("max_blocks", ct.c_int), ("matrix_powers", ct.c_int),
     ]
 
 
@@ -151,7 +151,7 @@ class Engine:
                  blocks_per_sm: int = 0, sell_sigma: int = 0, timeout_s: float = 0.0,
                  breakdown_tol: float = 0.0, matrix_format: str = "csr", sync_policy: int = 0,
                  col_staging: int = 0, keep_entry_map: bool = False, l2_window: int = 0,
-                 row_weight=None, diag_compensation: int = 0, matrix_powers: int = 0):
+                 row_weight=None, diag_compensation: int = 0, matrix_powers: int = 0, max_blocks: int = 0):
         self._lib = load_library()
         self._h = ct.c_void_p()
         n = A.shape[0]
@@ -211,6 +211,7 @@ class Engine:
         a.row_weight = _ptr(rw) if rw is not None else None
         a.diag_compensation = int(diag_compensation)
         a.matrix_powers = int(matrix_powers)
+        a.max_blocks = int(max_blocks)
         self._keep = (ptr, ind, val, U, Q, lam, flam, gamma, gs_re, gs_im, wts, shifts, cs, mass, ode, rw)
         rc = self._lib.gm_lanczos_create(ct.byref(a), ct.byref(self._h))
         self._keep = None
