@@ -46,9 +46,9 @@ struct gm_engine {
   int scale_exp = 0;             // mixed engine: A stored as A * 2^-scale_exp
   unsigned long long epoch = 0;  // launch counter (progress-flag epochs)
   double dep_avg = 0.0;          // mean neighbour-list length per block
-  int Gk[7] = {};                // grid size per phase group (co-residency bound)
-  void* kfn[7] = {};
-  size_t smem[7] = {};           // dynamic shared memory per phase group
+  int Gk[9] = {};                // grid size per phase group (co-residency bound)
+  void* kfn[9] = {};
+  size_t smem[9] = {};           // dynamic shared memory per phase group
   std::vector<DevBuf> bufs;
   size_t bytes = 0;
   KParams kp{};
@@ -413,7 +413,7 @@ int build_partition(gm_engine* e, const Csr& A, const std::vector<long long>& ro
   for (int p = 0; p < np; ++p) pb0[p + 1] = pb0[p] + gp[p];
   const int G = pb0[np];
   e->G = G;
-  for (int g = 0; g < 7; ++g) e->Gk[g] = G;   // every phase group
+  for (int g = 0; g < 9; ++g) e->Gk[g] = G;   // every phase group
   e->kp.G = G;
   std::vector<int> bs(G + 1, 0), bprob(G, 0);
   for (int p = 0; p < np; ++p) {
@@ -557,7 +557,7 @@ int build_partition(gm_engine* e, const Csr& A, const std::vector<long long>& ro
 // Phase-group kernels (kern_fp64.cu / kern_mixed.cu): 0 lanczos, 1 solves,
 // 2 apply, 3 deflate/update, 4 fused lanczos + solves + apply.
 enum { KGRP_LANCZOS = 0, KGRP_SOLVE = 1, KGRP_APPLY = 2, KGRP_DEFLATE = 3, KGRP_FUSED = 4,
-       KGRP_LANCZOS_MPK = 5, KGRP_FUSED_MPK = 6, KGRP_N = 7 };
+       KGRP_LANCZOS_MPK = 5, KGRP_FUSED_MPK = 6, KGRP_LANCZOS_RO = 7, KGRP_FUSED_RO = 8, KGRP_N = 9 };
 
 // The dynamic shared memory limit is an attribute of the kernel function,
 // shared by every handle of the process (per device): only ever raise it, so
@@ -615,7 +615,9 @@ int launch(gm_engine* e, int phases, int slot) {
   kp.phases = phases;
   void* args[] = {&kp};
   int grp = group_of(phases);
-  if (e->kp.mpk && (grp == KGRP_LANCZOS || grp == KGRP_FUSED))
+  if (e->kp.reorth > 0 && (grp == KGRP_LANCZOS || grp == KGRP_FUSED))
+    grp = grp == KGRP_LANCZOS ? KGRP_LANCZOS_RO : KGRP_FUSED_RO;
+  else if (e->kp.mpk && (grp == KGRP_LANCZOS || grp == KGRP_FUSED))
     grp = grp == KGRP_LANCZOS ? KGRP_LANCZOS_MPK : KGRP_FUSED_MPK;
   kp.G = e->Gk[grp];
   if (e->capturing) {
@@ -714,6 +716,7 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
   if (a->gamma_size < 1) return fail(e, GM_ERR_ARG, "lanczos_create:bad_gamma: gamma_size must be >= 1");
   if (a->contour_size < 1) return fail(e, GM_ERR_ARG, "lanczos_create:bad_gamma_s_real: contour size must be >= 1");
   if (a->precision != GM_FP64 && a->precision != GM_MIXED) return fail(e, GM_ERR_ARG, "unknown precision %d", a->precision);
+  if (a->reorth < 0 || a->reorth > 2) return fail(e, GM_ERR_ARG, "reorth must be 0 (none), 1 (CGS) or 2 (CGS2), got %d", a->reorth);
   long long ntot = 0;
   for (int p = 0; p < np; ++p) {
     const ProbIn& q = probs[p];
@@ -731,7 +734,9 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
 
   e->keep_map = a->keep_entry_map != 0 && np == 1;
   e->comp = a->precision == GM_MIXED && a->diag_compensation == 0;
-  e->mpk_req = a->matrix_powers != 0 && np == 1 && a->sell_sigma <= 1 && a->gamma_size >= 3;
+  // matrix-powers passes and reorthogonalisation are separate entry points;
+  // reorthogonalisation takes precedence
+  e->mpk_req = a->matrix_powers != 0 && np == 1 && a->sell_sigma <= 1 && a->gamma_size >= 3 && a->reorth == 0;
   if (e->comp && a->row_weight) {
     if (np != 1) return fail(e, GM_ERR_ARG, "row_weight applies to a single problem");
     e->roww.assign(a->row_weight, a->row_weight + probs[0].n);
@@ -803,7 +808,7 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
     e->kfn[g] = pick_kernel(e->prec, e->R, g);
     if (!e->kfn[g]) return fail(e, GM_ERR_UNSUPPORTED, "no kernel for nrhs %d", e->R);
     e->smem[g] = (g == KGRP_LANCZOS || g == KGRP_APPLY || g == KGRP_FUSED || g == KGRP_LANCZOS_MPK ||
-                  g == KGRP_FUSED_MPK) ? stage_smem : 0;
+                  g == KGRP_FUSED_MPK || g == KGRP_LANCZOS_RO || g == KGRP_FUSED_RO) ? stage_smem : 0;
     if (e->smem[g] > 48 * 1024)
       GM_CUDA(e, raise_smem_limit(e->dev, e->kfn[g], e->smem[g]));
     int nb = 0;
@@ -962,6 +967,11 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
   if ((rc = dalloc(e, &kp.tri, (size_t)4 * m * PR * C))) return rc;
   if ((rc = dalloc(e, &kp.Z, (size_t)(k + 4) * R))) return rc;
   if ((rc = dalloc(e, &kp.part, (size_t)(2 * R + (k + 4) * R) * e->G))) return rc;
+  kp.reorth = a->reorth;
+  if (kp.reorth > 0) {
+    if ((rc = dalloc(e, &kp.hpart, (size_t)2 * (m + 8) * R * e->G))) return rc;
+    if ((rc = dalloc(e, &kp.hblk, (size_t)e->G * (m + 1) * R))) return rc;
+  }
   if ((rc = dalloc(e, &kp.bar, 2 + 2 * (size_t)np))) return rc;
   if ((rc = dalloc(e, &kp.status, 1))) return rc;
   if ((rc = dalloc(e, &kp.meff, PR))) return rc;
@@ -1153,6 +1163,32 @@ int gm_get_aabb(gm_handle h, double* dst) {
           }
   }
   return rc;
+}
+
+int gm_get_basis(gm_handle h, double* dst) {
+  if (!h || !dst) return GM_ERR_ARG;
+  const size_t n = (size_t)h->n, m = (size_t)h->m, R = (size_t)h->R;
+  const size_t bsz = h->prec == GM_FP64 ? 8 : 4;
+  std::vector<unsigned char> raw(m * n * R * bsz);
+  GM_CUDA(h, cudaMemcpyAsync(raw.data(), h->kp.V, raw.size(), cudaMemcpyDeviceToHost, h->stream));
+  int rc = check_sync(h);
+  if (rc) return rc;
+  // device [m][n][R] in the storage type -> host n x m per right-hand side
+  for (size_t j = 0; j < m; ++j)
+    for (size_t i = 0; i < n; ++i)
+      for (size_t r = 0; r < R; ++r) {
+        const size_t q = (j * n + i) * R + r;
+        double v;
+        if (bsz == 8) {
+          std::memcpy(&v, raw.data() + q * 8, 8);
+        } else {
+          float f;
+          std::memcpy(&f, raw.data() + q * 4, 4);
+          v = (double)f;
+        }
+        dst[(r * m + j) * n + i] = v;
+      }
+  return GM_OK;
 }
 
 int gm_get_y(gm_handle h, double* yr, double* yi) {

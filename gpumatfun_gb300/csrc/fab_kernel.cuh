@@ -28,7 +28,8 @@ enum Phase : int {
   PH_LANCZOS = 1, PH_TRISOLVE = 2, PH_COEF = 4, PH_APPLY = 8,
   PH_UPDATE_FKPP = 16, PH_UPDATE_FHN = 32, PH_DEFLATE = 64,
   PH_APPLY_SET = 128,  // apply writes X = lift (fused solve) instead of X += lift
-  PH_MPK = 256         // compile-time only: entry points with matrix-powers Horner passes
+  PH_MPK = 256,        // compile-time only: entry points with matrix-powers Horner passes
+  PH_REORTH = 512      // compile-time only: entry points with Gram-Schmidt reorthogonalisation
 };
 
 struct KParams {
@@ -92,7 +93,11 @@ struct KParams {
   const long long* halo_ptr;  // [G + 1]
   const int* halo_rows;
   const int* lcol;            // per SELL slot
-                              // bulk copies (slices of at most stage_cap columns); 0: off
+  // Gram-Schmidt reorthogonalisation of each Lanczos vector against the
+  // stored basis: 0 = none (the reference's recurrence), 1 = CGS, 2 = CGS2
+  int reorth;
+  double* hpart;    // [2][m + 8][R][G] per-block partial dots
+  double* hblk;     // [G][m + 1][R] each block's totals
   int* status;
   int* meff;        // [R]
   unsigned long long timeout_ns;
@@ -542,7 +547,109 @@ __device__ __forceinline__ void grid_total_smem(const double* partials, int stri
   __syncthreads();
 }
 
-template <class Pol, int R, bool MPK>
+// Classical Gram-Schmidt of the step's work vector w (unrounded, in Hw)
+// against the stored basis V_0..V_j, kp.reorth times (1 = CGS, 2 = CGS2):
+//   h_t = V_t^T w  (t = 0..j; per-block partials, then every block totals the
+//                  group's partials in one fixed order: deterministic)
+//   w  <- w - sum_t h_t V_t
+// The dots run over tiles of TT basis vectors so that each V_t is read once
+// per dot pass with TT*R accumulators per thread.  Between passes w stays in
+// the accumulator precision in Hw; the last correction rounds it to storage
+// once (Wout) and accumulates ||w||^2 into bpa.  Consecutive passes use
+// alternate halves of hpart, so a block that runs ahead cannot overwrite
+// partials another block is still summing.
+template <class Pol, int R>
+__device__ bool reorth_step(const KParams& kp, const Ctx& c, const Grp& g, int j, typename Pol::HT* Hw,
+                            typename Pol::BT* Wout, typename Pol::AT (&bpa)[R]) {
+  using BT = typename Pol::BT;
+  using HT = typename Pol::HT;
+  using AT = typename Pol::AT;
+  constexpr int TT = 8 / R;
+  const long long n = kp.n;
+  const BT* const V = reinterpret_cast<const BT*>(kp.V);
+  const int G = kp.G;
+  double* const hb = kp.hblk + (long long)c.b() * (kp.m + 1) * R;   // this block's totals [t][r]
+  for (int q = 0; q < kp.reorth; ++q) {
+    double* const hp = kp.hpart + (long long)(q & 1) * (kp.m + TT) * R * G;   // [t][r][G]
+    for (int t0 = 0; t0 <= j; t0 += TT) {
+      AT acc[TT][R];
+#pragma unroll
+      for (int u = 0; u < TT; ++u)
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[u][r] = Pol::zero();
+      for (long long i = g.gt(kp); i < g.r1(kp); i += g.tt()) {
+        HT wh[R];
+        VecIO<R>::ld(Hw + i * R, wh);
+#pragma unroll
+        for (int u = 0; u < TT; ++u) {
+          if (t0 + u <= j) {
+            BT v[R];
+            VecIO<R>::ld(V + ((long long)(t0 + u) * n + i) * R, v);
+#pragma unroll
+            for (int r = 0; r < R; ++r) acc[u][r] = Pol::dot(acc[u][r], h_load_at<Pol>(wh[r]), v[r]);
+          }
+        }
+      }
+      double a[TT * R];
+#pragma unroll
+      for (int u = 0; u < TT; ++u)
+#pragma unroll
+        for (int r = 0; r < R; ++r) a[u * R + r] = Pol::to_d(acc[u][r]);
+      block_sum_store<TT * R>(a, hp + (long long)t0 * R * G + c.b(), G);
+    }
+    if (!group_bar(kp, g.p).sync()) return false;
+    for (int x = c.warp(); x < (j + 1) * R; x += c.nw()) {
+      const double* pp = hp + (long long)x * G + g.gb;
+      double t = 0.0;
+      for (int b = c.lane(); b < g.Gp; b += 32) t += pp[b];
+      t = warp_sum(t);
+      if (c.lane() == 0) hb[x] = t;
+    }
+    __syncthreads();
+    const bool last = q + 1 == kp.reorth;
+    for (long long i = g.gt(kp); i < g.r1(kp); i += g.tt()) {
+      HT wh[R];
+      VecIO<R>::ld(Hw + i * R, wh);
+      AT w[R];
+#pragma unroll
+      for (int r = 0; r < R; ++r) w[r] = h_load_at<Pol>(wh[r]);
+      // TT basis entries loaded before they are used: TT loads in flight per row
+      int t = 0;
+      for (; t + TT <= j + 1; t += TT) {
+        BT v[TT][R];
+#pragma unroll
+        for (int u = 0; u < TT; ++u) VecIO<R>::ld(V + ((long long)(t + u) * n + i) * R, v[u]);
+#pragma unroll
+        for (int u = 0; u < TT; ++u)
+#pragma unroll
+          for (int r = 0; r < R; ++r) w[r] = Pol::sub_mul(w[r], Pol::scalar(hb[(t + u) * R + r]), v[u][r]);
+      }
+      for (; t <= j; ++t) {
+        BT v[R];
+        VecIO<R>::ld(V + ((long long)t * n + i) * R, v);
+#pragma unroll
+        for (int r = 0; r < R; ++r) w[r] = Pol::sub_mul(w[r], Pol::scalar(hb[t * R + r]), v[r]);
+      }
+      if (last) {
+        BT wb[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+          wb[r] = Pol::to_b(w[r]);
+          bpa[r] = Pol::dot_self(bpa[r], w[r]);
+        }
+        VecIO<R>::st(Wout + i * R, wb);
+      } else {
+#pragma unroll
+        for (int r = 0; r < R; ++r) wh[r] = Pol::to_h(w[r]);
+        VecIO<R>::st(Hw + i * R, wh);
+      }
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+template <class Pol, int R, bool MPK, bool RO>
 __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, PassSync& ps, ColStage& cs) {
   using BT = typename Pol::BT;
   using HT = typename Pol::HT;
@@ -748,16 +855,24 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
       }
     }
     __syncthreads();
-    // pass B: w -= alpha_j v_j; beta_{j+1} = ||w||
+    // pass B: w -= alpha_j v_j; beta_{j+1} = ||w||  (after the optional
+    // Gram-Schmidt against V_0..V_j)
     {
       AT bpa[R];
 #pragma unroll
       for (int r = 0; r < R; ++r) bpa[r] = Pol::zero();
+      const bool ro = RO && kp.reorth > 0;
       for (long long i = g.gt(kp); i < g.r1(kp); i += g.tt()) {
         HT wh[R];
         BT wb[R], v[R];
         VecIO<R>::ld(Hw + i * R, wh);
         VecIO<R>::ld(src + i * R, v);   // w_j
+        if (ro) {
+#pragma unroll
+          for (int r = 0; r < R; ++r) wh[r] = Pol::to_h(Pol::sub_mul(h_load_at<Pol>(wh[r]), sh.al[r], v[r]));
+          VecIO<R>::st(Hw + i * R, wh);
+          continue;
+        }
 #pragma unroll
         for (int r = 0; r < R; ++r) {
           AT w = Pol::sub_mul(h_load_at<Pol>(wh[r]), sh.al[r], v[r]);
@@ -765,6 +880,9 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
           bpa[r] = Pol::dot_self(bpa[r], w);
         }
         VecIO<R>::st(Wout + i * R, wb);
+      }
+      if constexpr (RO) {
+        if (ro && !reorth_step<Pol, R>(kp, c, g, j, Hw, Wout, bpa)) return false;
       }
       double bp[R];
 #pragma unroll
@@ -1142,7 +1260,7 @@ __global__ void __launch_bounds__(GM_MAXT, (R >= 4 ? 1 : GM_MINB)) fab_kernel(KP
   };
   if ((PH & PH_LANCZOS) && (ph & PH_LANCZOS)) {
     if (!sep()) return;
-    if (!phase_lanczos<Pol, R, (PH & PH_MPK) != 0>(kp, c, g, ps, cs)) return;
+    if (!phase_lanczos<Pol, R, (PH & PH_MPK) != 0, (PH & PH_REORTH) != 0>(kp, c, g, ps, cs)) return;
   }
   if ((PH & PH_TRISOLVE) && (ph & PH_TRISOLVE)) {
     if (!sep()) return;

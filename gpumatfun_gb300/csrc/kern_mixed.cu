@@ -12,6 +12,8 @@ static void* group_ptr(int group) {
     case 4: return (void*)fab_kernel<Pol, R, KG_LANCZOS | KG_SOLVE | KG_APPLY>;
     case 5: return (void*)fab_kernel<Pol, R, KG_LANCZOS | PH_MPK>;
     case 6: return (void*)fab_kernel<Pol, R, KG_LANCZOS | KG_SOLVE | KG_APPLY | PH_MPK>;
+    case 7: return (void*)fab_kernel<Pol, R, KG_LANCZOS | PH_REORTH>;
+    case 8: return (void*)fab_kernel<Pol, R, KG_LANCZOS | KG_SOLVE | KG_APPLY | PH_REORTH>;
   }
   return nullptr;
 }

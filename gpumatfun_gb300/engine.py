@@ -35,7 +35,7 @@ EXPORTED_SYMBOLS = [
     "gm_phase_times", "gm_info", "gm_get_meff", "gm_last_error", "gm_version",
     "gm_lin_sys_solves_noalloc", "gm_batch_create", "gm_time_loop", "gm_fe_attach", "gm_fe_assemble",
     "gm_fe_gradient", "gm_get_solution_device", "gm_fe_forward", "gm_fe_backward",
-    "gm_fe_backward_stored",
+    "gm_fe_backward_stored", "gm_get_basis",
 ]
 
 _dp = ct.POINTER(ct.c_double)
@@ -63,7 +63,7 @@ class CreateArgs(ct.Structure):
         ("sync_policy", ct.c_int), ("col_staging", ct.c_int), ("keep_entry_map", ct.c_int),
         ("l2_window", ct.c_int),
         ("row_weight", _dp), ("diag_compensation", ct.c_int),
-        ("max_blocks", ct.c_int), ("matrix_powers", ct.c_int),
+        ("max_blocks", ct.c_int), ("matrix_powers", ct.c_int), ("reorth", ct.c_int),
     ]
 
 
@@ -99,7 +99,7 @@ def load_library(build_if_missing: bool = False) -> ct.CDLL:
     for name in ("gm_lanczos_delete", "gm_build_subspace", "gm_lin_sys_solves", "gm_apply_V",
                  "gm_update_U", "gm_update_U_monodomain", "gm_solve", "gm_sync"):
         getattr(lib, name).argtypes = [h]
-    for name in ("gm_get_U", "gm_get_xsol", "gm_get_aabb", "gm_get_update", "gm_get_solution"):
+    for name in ("gm_get_U", "gm_get_xsol", "gm_get_aabb", "gm_get_update", "gm_get_solution", "gm_get_basis"):
         getattr(lib, name).argtypes = [h, _dp]
     lib.gm_set_U.argtypes = [h, _dp]
     lib.gm_set_U_device.argtypes = [h, ct.c_void_p]
@@ -151,7 +151,8 @@ class Engine:
                  blocks_per_sm: int = 0, sell_sigma: int = 0, timeout_s: float = 0.0,
                  breakdown_tol: float = 0.0, matrix_format: str = "csr", sync_policy: int = 0,
                  col_staging: int = 0, keep_entry_map: bool = False, l2_window: int = 0,
-                 row_weight=None, diag_compensation: int = 0, matrix_powers: int = 0, max_blocks: int = 0):
+                 row_weight=None, diag_compensation: int = 0, matrix_powers: int = 0, max_blocks: int = 0,
+                 reorth: int = 0):
         self._lib = load_library()
         self._h = ct.c_void_p()
         n = A.shape[0]
@@ -212,6 +213,7 @@ class Engine:
         a.diag_compensation = int(diag_compensation)
         a.matrix_powers = int(matrix_powers)
         a.max_blocks = int(max_blocks)
+        a.reorth = int(reorth)
         self._keep = (ptr, ind, val, U, Q, lam, flam, gamma, gs_re, gs_im, wts, shifts, cs, mass, ode, rw)
         rc = self._lib.gm_lanczos_create(ct.byref(a), ct.byref(self._h))
         self._keep = None
@@ -275,6 +277,12 @@ class Engine:
         return yr.reshape(-1, self.m).T.copy(), yi.reshape(-1, self.m).T.copy()
 
     # -- additions
+    def get_basis(self) -> np.ndarray:
+        """The Krylov basis of the last build, shape (nrhs, m, n), as FP64."""
+        out = np.empty(self.R * self.m * self.n)
+        self._check(self._lib.gm_get_basis(self._h, _ptr(out)))
+        return out.reshape(self.R, self.m, self.n)
+
     def set_U(self, U):
         u = _f64(np.asarray(U).reshape(self.n, -1).T).reshape(-1)
         if u.size != self.n * self.R:
@@ -434,7 +442,7 @@ class BatchEngine(Engine):
 
     def __init__(self, problems: Sequence, precision: str | int = "fp64", sync: bool = True,
                  threads: int = 0, blocks_per_sm: int = 0, sell_sigma: int = 0, timeout_s: float = 0.0,
-                 sync_policy: int = 0, col_staging: int = 0, diag_compensation: int = 0):
+                 sync_policy: int = 0, col_staging: int = 0, diag_compensation: int = 0, reorth: int = 0):
         self._lib = load_library()
         self._h = ct.c_void_p()
         P0 = problems[0]
@@ -468,6 +476,7 @@ class BatchEngine(Engine):
         a.threads_per_block, a.blocks_per_sm, a.sell_sigma = threads, blocks_per_sm, sell_sigma
         a.barrier_timeout_s, a.sync_policy, a.col_staging = timeout_s, int(sync_policy), int(col_staging)
         a.diag_compensation = int(diag_compensation)
+        a.reorth = int(reorth)
         rc = self._lib.gm_batch_create(len(problems), arr, ct.byref(a), ct.byref(self._h))
         del keep
         if rc != 0:

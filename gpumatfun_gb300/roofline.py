@@ -25,6 +25,7 @@ class Sizes:
     C: int
     k: int
     mixed: bool = False
+    reorth: int = 0     # Gram-Schmidt passes per Lanczos step (0, 1 or 2)
 
     @property
     def vb(self):   # matrix value bytes
@@ -56,7 +57,20 @@ def lanczos_bytes(s: Sizes) -> float:
             tot += (s.d - 1) * (M + s.hb * nR + s.sb * nR + s.hb * nR)  # Horner: gather H, read V_j, write H
             tot += M + s.hb * nR + s.sb * nR + prev + s.sb * nR    # final: gather H, V_j, V_{j-1}, write W
         tot += 3 * s.sb * nR                                        # pass B: read W, V_j, write W
+        tot += reorth_step_bytes(s, j)
     return tot
+
+
+def reorth_step_bytes(s: Sizes, j: int) -> float:
+    """Gram-Schmidt of step j against V_0..V_j, s.reorth times: per pass the
+    dots read w (in the Horner buffer) and V_0..V_j, and the correction reads
+    w and V_0..V_j again and writes w (the last pass writes the work vector
+    in storage precision instead)."""
+    if s.reorth <= 0:
+        return 0.0
+    nR = float(s.n) * s.R
+    per = 2 * (j + 1) * s.sb * nR + 2 * s.hb * nR + s.hb * nR
+    return s.reorth * per + s.hb * nR   # + pass B writing w unrounded
 
 
 def solve_bytes(s: Sizes) -> float:
@@ -91,4 +105,5 @@ def fused_solve_flops(s: Sizes) -> float:
     spmv = 2.0 * s.nnz * s.R
     per_step = (s.d + 1) * spmv + 2.0 * s.n * s.R * (2 + s.d + 3)
     apply = 2.0 * s.n * s.R * s.m * (s.d + 1) + s.d * spmv
-    return s.m * per_step + apply
+    reorth = sum(s.reorth * 2 * 2.0 * s.n * s.R * (j + 1) for j in range(s.m))
+    return s.m * per_step + apply + reorth

@@ -129,6 +129,12 @@ typedef struct gm_create_args {
                                   in between in shared memory), where it applies:
                                   one problem, no sigma sorting, the vector fits
                                   shared memory; 0 = one level per pass            */
+  int reorth;                  /* Gram-Schmidt reorthogonalisation of every new
+                                  Lanczos vector against the stored basis, with
+                                  FP64 dot products: 0 = none (the reference's
+                                  three-term recurrence, default), 1 = classical
+                                  Gram-Schmidt once, 2 = twice (CGS2).  Adds
+                                  2 (resp. 4) reads of V_0..V_j per step.        */
 } gm_create_args;
 
 /* Fill *args with defaults (zeros, struct_version, sync_mode = 1, nrhs = 2). */
@@ -207,6 +213,13 @@ int gm_set_y(gm_handle h, const double* yreal, const double* yimag);
 
 /* Copies Yreal and Yimag (m x nrhs*C each) to the host (either may be NULL). */
 int gm_get_y(gm_handle h, double* yreal, double* yimag);
+
+/* Copies the Krylov basis V to the host as FP64: for each right-hand side r an
+ * n x m column-major block (dst[(r*m + j)*n + i] = v_j(i)); rows in the
+ * caller's order (stacked problems for a batch).  In the mixed engine these
+ * are the FP32-stored vectors.  The basis of build_subspace (lanczos.h:47,
+ * V), which the reference keeps on the device only. */
+int gm_get_basis(gm_handle h, double* dst);
 
 /* ---- additions with no reference counterpart ------------------------------ */
 

@@ -42,7 +42,7 @@ def deflate(Q: np.ndarray, U: np.ndarray, flam: np.ndarray):
     return U, Q @ Z
 
 
-def lanczos(A: sp.spmatrix, U: np.ndarray, m: int, gamma: np.ndarray):
+def lanczos(A: sp.spmatrix, U: np.ndarray, m: int, gamma: np.ndarray, reorth: int = 0):
     """Polynomial-preconditioned Lanczos, one recurrence per column of U.
 
     Follows build_subspace.cu:5-89 (and its CPU twin lanczos.m:21-53):
@@ -50,7 +50,11 @@ def lanczos(A: sp.spmatrix, U: np.ndarray, m: int, gamma: np.ndarray):
     Horner u = p(A) v_j with p(x) = sum_i gamma_i x^(d-i) (:30-47),
     w = A u (:50); w -= beta_j v_{j-1} (j > 0, :53-60); alpha_j = w.v_j (:63-64);
     w -= alpha_j v_j (:67-72); beta_{j+1} = ||w|| (:75-76);
-    v_{j+1} = w * (1/beta_{j+1}) (j < m-1, :79-88).  No reorthogonalisation.
+    v_{j+1} = w * (1/beta_{j+1}) (j < m-1, :79-88).  The reference does no
+    reorthogonalisation (reorth = 0).  The engine's optional classical
+    Gram-Schmidt (reorth = 1, or 2 for CGS2) runs after w -= alpha_j v_j and
+    before beta_{j+1} = ||w||: w -= V_{0..j} (V_{0..j}^T w), reorth times;
+    alpha and beta keep their three-term values.
 
     Returns V (R, m, n), alpha (R, m), beta (R, m+1).
     """
@@ -75,6 +79,10 @@ def lanczos(A: sp.spmatrix, U: np.ndarray, m: int, gamma: np.ndarray):
         a = np.einsum("nr,nr->r", W, vj)
         alpha[:, j] = a
         W = W - a[None, :] * vj
+        for _ in range(reorth):
+            for r in range(R):
+                Vr = V[r, : j + 1]                 # (j+1, n)
+                W[:, r] = W[:, r] - Vr.T @ (Vr @ W[:, r])
         beta[:, j + 1] = np.linalg.norm(W, axis=0)
         if j != m - 1:
             V[:, j + 1, :] = (W * (1.0 / beta[:, j + 1])[None, :]).T
@@ -238,6 +246,7 @@ class OracleEngine:
     ode: np.ndarray | None = None
     fhn: tuple = (0.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0)  # aode,bode,code,vrest,vamp,vth,vpeak,c1ion
     apply_mode: str = "collapsed"
+    reorth: int = 0
     V: np.ndarray = field(default=None, init=False)
     alpha: np.ndarray = field(default=None, init=False)
     beta: np.ndarray = field(default=None, init=False)
@@ -265,7 +274,7 @@ class OracleEngine:
         return self.U.shape[1]
 
     def build_subspace(self):
-        self.V, self.alpha, self.beta = lanczos(self.A, self.U, self.m, self.gamma)
+        self.V, self.alpha, self.beta = lanczos(self.A, self.U, self.m, self.gamma, self.reorth)
 
     def lin_sys_solves(self):
         self.Yr, self.Yi = tridiag_solves(self.alpha, self.beta, self.wts, self.shifts, self.m)

@@ -108,3 +108,23 @@ def test_update_U_semantics():
     u = np.where(u >= 0, u, 0.0)
     np.testing.assert_allclose(U[:, 0], u)
     np.testing.assert_allclose(U[:, 1], 0.1 * mass * (u / mass) * (1 - u / mass))
+
+
+@pytest.mark.parametrize("reorth", [1, 2])
+def test_oracle_reorth_keeps_basis_orthonormal(reorth):
+    """Degree 3, m = 40: the plain recurrence's basis loses orthogonality;
+    Gram-Schmidt keeps it at rounding level, and f(A)b is unchanged to the
+    method's accuracy (both agree with the exact DST solution)."""
+    N = 20
+    P = workloads.config1_small(N=N, k=3, m=40, C=20, R=1, degree=3, seed=3)
+    ex = known.dst_fab_2d(P.U[:, 0], N, P.funcs[0], scale=(N + 1.0) ** 2)
+    out = {}
+    for ro in (0, reorth):
+        o = fab.OracleEngine(A=P.A, U0=P.U, Q=P.Q, m=P.m, gamma=P.gamma, gs_re=P.gs_re, gs_im=P.gs_im,
+                             flam=P.flam, wts=P.wts, shifts=P.shifts, col_scale=np.ones(1), reorth=ro)
+        x = o.solve()[:, 0]
+        V = o.V[0]
+        out[ro] = (np.abs(V @ V.T - np.eye(P.m)).max(), np.linalg.norm(x - ex) / np.linalg.norm(ex))
+    assert out[0][0] > 1e-2
+    assert out[reorth][0] < 1e-14
+    assert out[0][1] < 1e-11 and out[reorth][1] < 1e-11
