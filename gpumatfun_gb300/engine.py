@@ -64,6 +64,7 @@ class CreateArgs(ct.Structure):
         ("l2_window", ct.c_int),
         ("row_weight", _dp), ("diag_compensation", ct.c_int),
         ("max_blocks", ct.c_int), ("matrix_powers", ct.c_int), ("reorth", ct.c_int),
+        ("val_prefetch", ct.c_int),
     ]
 
 
@@ -152,7 +153,7 @@ class Engine:
                  breakdown_tol: float = 0.0, matrix_format: str = "csr", sync_policy: int = 0,
                  col_staging: int = 0, keep_entry_map: bool = False, l2_window: int = 0,
                  row_weight=None, diag_compensation: int = 0, matrix_powers: int = 0, max_blocks: int = 0,
-                 reorth: int = 0):
+                 reorth: int = 0, val_prefetch: int = 0):
         self._lib = load_library()
         self._h = ct.c_void_p()
         n = A.shape[0]
@@ -214,6 +215,7 @@ class Engine:
         a.matrix_powers = int(matrix_powers)
         a.max_blocks = int(max_blocks)
         a.reorth = int(reorth)
+        a.val_prefetch = int(val_prefetch)
         self._keep = (ptr, ind, val, U, Q, lam, flam, gamma, gs_re, gs_im, wts, shifts, cs, mass, ode, rw)
         rc = self._lib.gm_lanczos_create(ct.byref(a), ct.byref(self._h))
         self._keep = None
@@ -375,10 +377,11 @@ class Engine:
     nprob = 1
 
     def info(self) -> dict:
-        v = (ct.c_int64 * 14)()
+        v = (ct.c_int64 * 16)()
         self._check(self._lib.gm_info(self._h, v))
         keys = ("n", "nrhs", "m", "d", "C", "k", "precision", "grid_blocks", "threads",
-                "sell_padded", "device_bytes", "launches", "problems", "matrix_powers")
+                "sell_padded", "device_bytes", "launches", "problems", "matrix_powers",
+                "value_prefetch_bytes", "reorth")
         return dict(zip(keys, list(v)))
 
     def meff(self) -> list:
@@ -442,7 +445,8 @@ class BatchEngine(Engine):
 
     def __init__(self, problems: Sequence, precision: str | int = "fp64", sync: bool = True,
                  threads: int = 0, blocks_per_sm: int = 0, sell_sigma: int = 0, timeout_s: float = 0.0,
-                 sync_policy: int = 0, col_staging: int = 0, diag_compensation: int = 0, reorth: int = 0):
+                 sync_policy: int = 0, col_staging: int = 0, diag_compensation: int = 0, reorth: int = 0,
+                 val_prefetch: int = 0):
         self._lib = load_library()
         self._h = ct.c_void_p()
         P0 = problems[0]
@@ -477,6 +481,7 @@ class BatchEngine(Engine):
         a.barrier_timeout_s, a.sync_policy, a.col_staging = timeout_s, int(sync_policy), int(col_staging)
         a.diag_compensation = int(diag_compensation)
         a.reorth = int(reorth)
+        a.val_prefetch = int(val_prefetch)
         rc = self._lib.gm_batch_create(len(problems), arr, ct.byref(a), ct.byref(self._h))
         del keep
         if rc != 0:

@@ -7,7 +7,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
   if (nrhs != 4) mexErrMsgIdAndTxt("MATLAB:fe_backward:invalidNumInputs", "Four input arguments are required.");
   if (nlhs < 1 || nlhs > 2) mexErrMsgIdAndTxt("MATLAB:fe_backward:maxlhs", "One or two output arguments are required.");
   gm_handle h = gm_mex_handle(prhs[0], "fe_backward");
-  int64_t info[16];  /* gm_info writes 14 entries */
+  int64_t info[16];  /* gm_info writes 16 entries */
   gm_mex_check(gm_info(h, info), h, "fe_backward");
   const size_t n = (size_t)info[0];
   for (int i = 1; i < 4; ++i)

@@ -5,7 +5,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
   if (nrhs != 3) mexErrMsgIdAndTxt("MATLAB:fe_forward:invalidNumInputs", "Three input arguments are required.");
   if (nlhs != 1) mexErrMsgIdAndTxt("MATLAB:fe_forward:maxlhs", "One output argument is required.");
   gm_handle h = gm_mex_handle(prhs[0], "fe_forward");
-  int64_t info[16];  /* gm_info writes 14 entries */
+  int64_t info[16];  /* gm_info writes 16 entries */
   gm_mex_check(gm_info(h, info), h, "fe_forward");
   if (!mxIsDouble(prhs[1]) || !mxIsDouble(prhs[2]) || mxGetNumberOfElements(prhs[2]) != (size_t)info[0])
     mexErrMsgIdAndTxt("MATLAB:fe_forward:badInput", "kappa and b must be real doubles, b with n entries.");

@@ -4,7 +4,7 @@
 void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
   if (nrhs != 1 || nlhs != 1) mexErrMsgIdAndTxt("MATLAB:get_aabb:invalidNumInputs", "Handle input argument required.");
   gm_handle h = gm_mex_handle(prhs[0], "get_aabb");
-  int64_t info[16];  /* gm_info writes 14 entries */
+  int64_t info[16];  /* gm_info writes 16 entries */
   gm_mex_check(gm_info(h, info), h, "get_aabb");
   plhs[0] = mxCreateDoubleMatrix((mwSize)(info[2] + 1), (mwSize)(2 * info[1]), mxREAL);
   gm_mex_check(gm_get_aabb(h, mxGetPr(plhs[0])), h, "get_aabb");

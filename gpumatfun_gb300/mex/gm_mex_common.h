@@ -40,7 +40,7 @@ static void gm_mex_check(int rc, gm_handle h, const char* fn) {
     if (nrhs != 1) mexErrMsgIdAndTxt("MATLAB:" FN ":invalidNumInputs", "Handle input argument required."); \
     if (nlhs != 1) mexErrMsgIdAndTxt("MATLAB:" FN ":maxlhs", "One output arguments is required."); \
     gm_handle h = gm_mex_handle(prhs[0], FN);                                          \
-    int64_t info[16];  /* gm_info writes 14 entries */                                                                  \
+    int64_t info[16];  /* gm_info writes 16 entries */                                                                  \
     gm_mex_check(gm_info(h, info), h, FN);                                             \
     plhs[0] = mxCreateDoubleMatrix((mwSize)info[0], (mwSize)info[1], mxREAL);         \
     gm_mex_check(CALL(h, mxGetPr(plhs[0])), h, FN);                                    \

@@ -4,7 +4,7 @@
 void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
   if (nrhs != 3 || nlhs != 0) mexErrMsgIdAndTxt("MATLAB:set_y:invalidNumInputs", "Handle, yreal and yimag required.");
   gm_handle h = gm_mex_handle(prhs[0], "set_y");
-  int64_t info[16];  /* gm_info writes 14 entries */
+  int64_t info[16];  /* gm_info writes 16 entries */
   gm_mex_check(gm_info(h, info), h, "set_y");
   const size_t want = (size_t)info[2] * info[1] * info[4];
   if (!mxIsDouble(prhs[1]) || !mxIsDouble(prhs[2]) || mxGetNumberOfElements(prhs[1]) != want ||

@@ -135,6 +135,11 @@ typedef struct gm_create_args {
                                   three-term recurrence, default), 1 = classical
                                   Gram-Schmidt once, 2 = twice (CGS2).  Adds
                                   2 (resp. 4) reads of V_0..V_j per step.        */
+  int val_prefetch;            /* L2 bulk prefetch (TMA) of each slice's values
+                                  with its column copy: 0 = when the matrix is not
+                                  held in the L2 persisting window (default),
+                                  1 = always, 2 = never.  More bytes in flight per
+                                  warp for a matrix streamed from HBM.           */
 } gm_create_args;
 
 /* Fill *args with defaults (zeros, struct_version, sync_mode = 1, nrhs = 2). */
@@ -320,8 +325,10 @@ int gm_phase_times(gm_handle h, float* ms5);
 /* Engine facts: [0] n, [1] nrhs, [2] m, [3] d, [4] C, [5] k, [6] precision,
  * [7] grid blocks, [8] threads per block, [9] SELL padded entries,
  * [10] device bytes held, [11] kernel launches so far, [12] problems,
- * [13] 1 when matrix-powers passes are active.  info has 14 entries. */
-int gm_info(gm_handle h, int64_t* info14);
+ * [13] 1 when matrix-powers passes are active, [14] bytes per SELL value
+ * when the values are prefetched into L2 (0: no prefetch), [15] Gram-Schmidt passes per
+ * Lanczos step.  info has 16 entries. */
+int gm_info(gm_handle h, int64_t* info16);
 
 /* Effective Krylov dimension per (problem, RHS) after the last build (< m
  * after a breakdown). */
