@@ -2,7 +2,11 @@
  * Same 26 positional arguments (U, A, Q, lambda, N, gamma, gamma_s_real,
  * gamma_s_imag, exp_lambda, phi_lambda, dt, ode, aode, bode, code, vrest,
  * vamp, vth, vpeak, c1ion, c2ion, mass, wts1, wts2, shifts, valvec) and the
- * same error identifiers; returns the engine handle as a 1x1 uint64. */
+ * same error identifiers; returns the engine handle as a 1x1 uint64.
+ * An optional 27th argument, a struct, sets engine options by field name:
+ * precision ('fp64' | 'mixed'), reorth, val_prefetch, matrix_powers,
+ * sync_policy, threads_per_block, blocks_per_sm, sell_sigma (numbers as
+ * gm_create_args documents them); absent fields keep their defaults. */
 #include <vector>
 #include "gm_mex_common.h"
 
@@ -15,8 +19,33 @@ static double scalar_arg(const mxArray* a, const char* id) {
   return mxGetScalar(a);
 }
 
+static void read_options(const mxArray* o, gm_create_args* a) {
+  if (!mxIsStruct(o)) mexErrMsgIdAndTxt("MATLAB:lanczos_create:badOptions", "Options must be a struct.");
+  const mxArray* p = mxGetField(o, 0, "precision");
+  if (p) {
+    if (!mxIsChar(p)) mexErrMsgIdAndTxt("MATLAB:lanczos_create:badOptions", "precision must be 'fp64' or 'mixed'.");
+    char* s = mxArrayToString(p);
+    const bool mixed = s && strcmp(s, "mixed") == 0, fp64 = s && strcmp(s, "fp64") == 0;
+    mxFree(s);
+    if (!mixed && !fp64) mexErrMsgIdAndTxt("MATLAB:lanczos_create:badOptions", "precision must be 'fp64' or 'mixed'.");
+    a->precision = mixed ? GM_MIXED : GM_FP64;
+  }
+  struct { const char* name; int* dst; } ints[] = {
+      {"reorth", &a->reorth}, {"val_prefetch", &a->val_prefetch}, {"matrix_powers", &a->matrix_powers},
+      {"sync_policy", &a->sync_policy}, {"threads_per_block", &a->threads_per_block},
+      {"blocks_per_sm", &a->blocks_per_sm}, {"sell_sigma", &a->sell_sigma}};
+  for (auto& f : ints) {
+    const mxArray* v = mxGetField(o, 0, f.name);
+    if (!v) continue;
+    if (!mxIsDouble(v) || mxGetNumberOfElements(v) != 1)
+      mexErrMsgIdAndTxt("MATLAB:lanczos_create:badOptions", "Option %s must be a numeric scalar.", f.name);
+    *f.dst = (int)mxGetScalar(v);
+  }
+}
+
 void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
-  if (nrhs != 26) mexErrMsgIdAndTxt("MATLAB:lanczos_create:invalidNumInputs", "Twenty-five input arguments are required.");
+  if (nrhs != 26 && nrhs != 27)
+    mexErrMsgIdAndTxt("MATLAB:lanczos_create:invalidNumInputs", "Twenty-five input arguments are required.");
   if (nlhs != 1) mexErrMsgIdAndTxt("MATLAB:lanczos_create:maxlhs", "One output argument is required.");
   const mxArray *U = prhs[0], *A = prhs[1], *Q = prhs[2];
   if (!mxIsDouble(U) || mxIsComplex(U)) mexErrMsgIdAndTxt("MATLAB:lanczos_create:badU", "Invalid U input argument.");
@@ -82,6 +111,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
   a.shifts = mxGetPr(prhs[24]);
   /* prhs[25] is valvec = [-1 0 1]: the reference keeps BLAS scalars on the
    * device; the engine needs none. */
+  if (nrhs == 27) read_options(prhs[26], &a);
   gm_handle h = nullptr;
   int rc = gm_lanczos_create(&a, &h);
   if (rc != GM_OK) mexErrMsgIdAndTxt("MATLAB:lanczos_create:engine", "%s", gm_last_error(nullptr));

@@ -26,4 +26,9 @@ size_t mxGetNumberOfElements(const mxArray*);
 double mxGetScalar(const mxArray*);
 mxArray* mxCreateDoubleMatrix(mwSize, mwSize, mxComplexity);
 mxArray* mxCreateNumericMatrix(mwSize, mwSize, mxClassID, mxComplexity);
+bool mxIsStruct(const mxArray*);
+bool mxIsChar(const mxArray*);
+mxArray* mxGetField(const mxArray*, mwIndex, const char*);
+char* mxArrayToString(const mxArray*);
+void mxFree(void*);
 }
