@@ -231,13 +231,16 @@ __device__ __forceinline__ void spmv_slot(const KParams& kp, long long s, int la
   constexpr int CH = ChunkWidth<VT, XT, R>::value;
   const long long base = kp.slice_off[s];
   const int len = (int)((kp.slice_off[s + 1] - base) >> 5);
-  // Column indices through one generic pointer, to the shared-memory stage
-  // when the slice is staged, else to global memory: one load form in the
-  // chunk loop instead of a select between two (measured 19% faster on the
-  // HBM-streamed 3D matrix, within 1.3% on the L2-resident FE matrix).
-  // Values from global memory (read-only path; with value prefetch they are
-  // already on their way into L2).
-  const int* cp = scol ? scol + lane : (colarr ? colarr : kp.col) + base + lane;
+  // Column indices from the shared-memory stage when the slice is staged,
+  // else from global memory, chosen by a warp-uniform branch per chunk;
+  // values from global memory (read-only path; with value prefetch they are
+  // already on their way into L2).  Measured against the two other shapes of
+  // this loop (a per-load select of the source, and one generic pointer for
+  // both): 1M FE disk FP64 44.6 vs 42.8 / 42.4 solves/s, mixed 57.1 vs 55.7;
+  // the generic pointer is faster only for FP64 on the HBM-streamed 3D
+  // matrix (17.2 vs 15.8), whose reference precision is the mixed engine
+  // (19.6 vs 19.3 here).
+  const int* gcp = (colarr ? colarr : kp.col) + base + lane;
   const VT* vp = reinterpret_cast<const VT*>(kp.val) + base + lane;
 #pragma unroll
   for (int r = 0; r < R; ++r) acc[r] = Pol::zero();
@@ -251,16 +254,15 @@ __device__ __forceinline__ void spmv_slot(const KParams& kp, long long s, int la
   for (int jj = 0; jj < len; jj += CH) {
     int cc[CH];
     VT aa[CH];
+    if (scol) {
 #pragma unroll
-    for (int u = 0; u < CH; ++u) {
-      if (jj + u < len) {
-        cc[u] = cp[(jj + u) * 32];
-        aa[u] = __ldg(vp + (long long)(jj + u) * 32);
-      } else {
-        cc[u] = 0;
-        aa[u] = (VT)0;
-      }
+      for (int u = 0; u < CH; ++u) cc[u] = jj + u < len ? scol[(jj + u) * 32 + lane] : 0;
+    } else {
+#pragma unroll
+      for (int u = 0; u < CH; ++u) cc[u] = jj + u < len ? __ldg(gcp + (long long)(jj + u) * 32) : 0;
     }
+#pragma unroll
+    for (int u = 0; u < CH; ++u) aa[u] = jj + u < len ? __ldg(vp + (long long)(jj + u) * 32) : (VT)0;
     XT xv[CH][R];
 #pragma unroll
     for (int u = 0; u < CH; ++u)
