@@ -124,15 +124,26 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def profiled_traffic(workload: str):
-    """DRAM bytes per fused launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", f"fab_fused_{workload}.md")
+def profiled_traffic(workload: str, precision: str, nrhs: int):
+    """DRAM bytes per fused launch of this workload from the committed ncu
+    summaries: a line ``traffic[<workload>/<precision>/R<nrhs>]: <bytes>`` in
+    profiles/*.md (measured on that launch, or scaled from a smaller capture
+    of the same kernel, as the summary says)."""
+    base = workload[:-len("-mixed")] if workload.endswith("-mixed") else workload
+    base = base[:-len("-fp64")] if base.endswith("-fp64") else base
+    key = f"traffic[{base}/{precision}/R{nrhs}]:"
+    pdir = os.path.join(ROOT, "profiles")
     try:
-        for line in open(path):
-            if line.startswith("dram_bytes_per_launch:"):
-                return float(line.split(":")[1])
+        names = sorted(os.listdir(pdir))
     except OSError:
-        pass
+        return None
+    for name in names:
+        if not name.endswith(".md"):
+            continue
+        with open(os.path.join(pdir, name)) as fh:
+            for line in fh:
+                if line.startswith(key):
+                    return float(line.split(":", 1)[1])
     return None
 
 
@@ -297,7 +308,7 @@ def run_ours(args, P, rank, world, local):
     peak, peak_kind = measured_peaks()
     achieved = alg / (ms_fused * 1e-3) / 1e9
     # the committed ncu summary covers the FP64 single-RHS launch of this workload
-    traffic = profiled_traffic(P.name) if (args.precision == "fp64" and R == 1 and args.reorth == 0) else None
+    traffic = profiled_traffic(P.name, args.precision, R) if args.reorth == 0 else None
     roof = {"bound": "hbm", "kernel": "fab_kernel (fused Lanczos + shifted solves + lift)",
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_kind": f"{peak_kind} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
