@@ -24,6 +24,7 @@ import scipy.sparse as sp
 __all__ = [
     "tridiag_1d", "laplacian_2d", "laplacian_2d_eigpairs", "laplacian_3d_var",
     "FEMesh", "disk_mesh", "gaussian_random_field", "p1_assemble", "fe_operator",
+    "FEFixture", "load_fe_mat",
 ]
 
 
@@ -228,3 +229,45 @@ def fe_operator(mesh: FEMesh, kappa: np.ndarray):
     A = sp.csr_matrix(D @ K @ D)
     A.sort_indices()
     return A, ms, inner
+
+
+@dataclass
+class FEFixture:
+    """An FE problem read from a MATLAB mesh file of the reference's form."""
+    A: sp.csr_matrix       # M^{-1/2} K M^{-1/2} on the kept nodes
+    msqrt: np.ndarray      # sqrt of the lumped mass on the kept nodes
+    nodes: np.ndarray      # (nn, dim) coordinates of all nodes
+    elements: np.ndarray   # (ne, 3) zero-based node indices
+    kept: np.ndarray       # zero-based indices of the kept nodes
+
+
+def load_fe_mat(path: str, dirichlet: bool = True) -> FEFixture:
+    """Read K, M, nodes and elements from a MATLAB v5 .mat mesh (the layout of
+    the reference's circle1/2/3.mat, read by process_nonuniform.m:12) and form
+    A = diag(1/sqrt(diag M)) K diag(1/sqrt(diag M)) as process_nonuniform.m:90-91
+    does.  With ``dirichlet`` (default) the operator is restricted to the
+    file's ``internal_nodes`` (homogeneous Dirichlet), which makes it SPD;
+    otherwise every node is kept (the reference's Neumann operator, singular).
+    The reference's symrcm reordering (process_nonuniform.m:15-20) is not
+    applied: the engine partitions and orders rows itself."""
+    import scipy.io as sio
+    d = sio.loadmat(path)
+    for key in ("K", "M", "nodes", "elements"):
+        if key not in d:
+            raise ValueError(f"{path}: no variable {key!r}")
+    K = sp.csr_matrix(d["K"], dtype=np.float64)
+    Mdiag = np.asarray(sp.csr_matrix(d["M"]).diagonal(), dtype=np.float64).ravel()
+    n = K.shape[0]
+    if dirichlet:
+        if "internal_nodes" not in d:
+            raise ValueError(f"{path}: no variable 'internal_nodes' for the Dirichlet restriction")
+        kept = np.asarray(d["internal_nodes"]).ravel().astype(np.int64) - 1   # MATLAB is one-based
+    else:
+        kept = np.arange(n, dtype=np.int64)
+    Kk = K[kept][:, kept]
+    ms = np.sqrt(Mdiag[kept])
+    D = sp.diags(1.0 / ms)
+    A = sp.csr_matrix(D @ Kk @ D)
+    A.sort_indices()
+    elements = np.asarray(d["elements"]).astype(np.int64) - 1
+    return FEFixture(A=A, msqrt=ms, nodes=np.asarray(d["nodes"], dtype=np.float64), elements=elements, kept=kept)

@@ -17,9 +17,7 @@ import os
 import sys
 
 import numpy as np
-import scipy.io as sio
 import scipy.linalg as sla
-import scipy.sparse as sp
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
@@ -28,14 +26,8 @@ REF = os.environ.get("GPUMATFUN_REF", "/root/reference")
 
 
 def circle_case(name, seed):
-    d = sio.loadmat(os.path.join(REF, name + ".mat"))
-    K = sp.csr_matrix(d["K"])
-    M = np.asarray(sp.csr_matrix(d["M"]).diagonal()).ravel()
-    inner = np.asarray(d["internal_nodes"]).ravel().astype(np.int64) - 1
-    Ki = K[inner][:, inner]
-    ms = np.sqrt(M[inner])
-    A = sp.csr_matrix(sp.diags(1 / ms) @ Ki @ sp.diags(1 / ms))
-    A.sort_indices()
+    from gpumatfun_gb300.problems import load_fe_mat
+    A = load_fe_mat(os.path.join(REF, name + ".mat")).A
     Ad = A.toarray()
     lam, Qf = sla.eigh(0.5 * (Ad + Ad.T))
     rng = np.random.default_rng(seed)
