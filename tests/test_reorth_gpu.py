@@ -140,3 +140,26 @@ def test_reorth_argument_checked(engine_lib):
     P = workloads.config1_small(N=8, k=2, m=6, C=8, R=1, degree=0, seed=1)
     with pytest.raises(GmError, match="reorth"):
         Engine.from_problem(P, reorth=3)
+
+
+@pytest.mark.parametrize("reorth", [1, 2])
+def test_reorth_breakdown_invariant_subspace(engine_lib, reorth):
+    """b on 3 coordinates of a diagonal A: the Krylov space is 3-dimensional;
+    Gram-Schmidt leaves beta_3 at rounding level, the default tolerance stops
+    the recurrence at m_eff = 3 and f(A)b is exact."""
+    import scipy.sparse as sp
+    n = 64
+    d = np.linspace(1.0, 10.0, n)
+    A = sp.diags(d).tocsr()
+    b = np.zeros(n)
+    b[[3, 20, 50]] = [1.0, -2.0, 0.5]
+    f = params.frac_power(-0.8)
+    P = workloads.make_problem("diag", A, b[:, None], np.zeros((n, 0)), np.zeros(0), [f], m=12, C=40,
+                               l1=0.9, lN=11.0, degree=0)
+    eng = Engine.from_problem(P, reorth=reorth)
+    eng.solve()
+    assert eng.meff()[0] == 3
+    assert rel(eng.get_solution()[:, 0], f(d) * b) < 1e-9
+    V = eng.get_basis()[0]
+    assert orth_loss(V[:3]) < 1e-14
+    eng.delete()
