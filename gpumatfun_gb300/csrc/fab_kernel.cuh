@@ -597,6 +597,18 @@ __device__ __forceinline__ void grid_total_smem(const double* partials, int stri
   __syncthreads();
 }
 
+// The per-block Gram-Schmidt coefficient x as the policy's scalar: FP64, or
+// the float-float pair stored in the same 8 bytes.
+template <class Pol>
+__device__ __forceinline__ typename Pol::ST reorth_scalar(const double* hb, int x) {
+  if constexpr (Pol::kMixed) {
+    const float2 f = reinterpret_cast<const float2*>(hb)[x];
+    return ff{f.x, f.y};
+  } else {
+    return hb[x];
+  }
+}
+
 // Classical Gram-Schmidt of the step's work vector w (unrounded, in Hw)
 // against the stored basis V_0..V_j, kp.reorth times (1 = CGS, 2 = CGS2):
 //   h_t = V_t^T w  (t = 0..j; per-block partials, then every block totals the
@@ -653,7 +665,16 @@ __device__ bool reorth_step(const KParams& kp, const Ctx& c, const Grp& g, int j
       double t = 0.0;
       for (int b = c.lane(); b < g.Gp; b += 32) t += pp[b];
       t = warp_sum(t);
-      if (c.lane() == 0) hb[x] = t;
+      if (c.lane() == 0) {
+        // the correction's scalar, once per block: float-float for the
+        // mixed engine (no double conversions per element)
+        if constexpr (Pol::kMixed) {
+          const ff hv = ff_from_double(t);
+          reinterpret_cast<float2*>(hb)[x] = make_float2(hv.hi, hv.lo);
+        } else {
+          hb[x] = t;
+        }
+      }
     }
     __syncthreads();
     const bool last = q + 1 == kp.reorth;
@@ -672,13 +693,13 @@ __device__ bool reorth_step(const KParams& kp, const Ctx& c, const Grp& g, int j
 #pragma unroll
         for (int u = 0; u < TT; ++u)
 #pragma unroll
-          for (int r = 0; r < R; ++r) w[r] = Pol::sub_mul(w[r], Pol::scalar(hb[(t + u) * R + r]), v[u][r]);
+          for (int r = 0; r < R; ++r) w[r] = Pol::sub_mul(w[r], reorth_scalar<Pol>(hb, (t + u) * R + r), v[u][r]);
       }
       for (; t <= j; ++t) {
         BT v[R];
         VecIO<R>::ld(V + ((long long)t * n + i) * R, v);
 #pragma unroll
-        for (int r = 0; r < R; ++r) w[r] = Pol::sub_mul(w[r], Pol::scalar(hb[t * R + r]), v[r]);
+        for (int r = 0; r < R; ++r) w[r] = Pol::sub_mul(w[r], reorth_scalar<Pol>(hb, t * R + r), v[r]);
       }
       if (last) {
         BT wb[R];
