@@ -315,6 +315,15 @@ def run_ours(args, P, rank, world, local):
             else "fallback 6.8 TB/s", "traffic": traffic, "algorithmic_bytes_per_launch": alg,
             "ms_per_launch": ms_fused,
             "fp64_tflops": roofline.fused_solve_flops(sizes) / (ms_fused * 1e-3) / 1e12}
+    if args.precision == "fp64":
+        # the FP64 pipe is the binding unit on GB300 (2 FMA lanes per clock per
+        # SM); its peak at the SM clock sampled during the timed region
+        mhz = (clocks or {}).get("sm_mhz") or 0.0
+        nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+        if mhz:
+            peak64 = 2 * 2 * nsm * mhz * 1e6 / 1e12
+            roof["fp64_peak_tflops"] = peak64
+            roof["fp64_frac"] = roof["fp64_tflops"] / peak64
 
     line = {"metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
