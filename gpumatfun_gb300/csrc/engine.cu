@@ -149,7 +149,7 @@ __global__ void k_pack_in(const double* __restrict__ cm, double* __restrict__ il
   if (t >= n * R) return;
   const long long i = t / R;
   const int r = (int)(t % R);
-  il[t] = cm[(long long)r * n + i] * scale[r];
+  il[t] = scale ? cm[(long long)r * n + i] * scale[r] : cm[(long long)r * n + i];
 }
 
 __global__ void k_pack_out(const double* __restrict__ il, double* __restrict__ cm, long long n, int R) {
@@ -670,7 +670,7 @@ int copy_out(gm_engine* e, const double* src_il, double* dst) {
 }
 
 // Usol <- U (column-major n x R, host or device) scaled by col_scale.
-int set_usol(gm_engine* e, const double* U, bool on_device) {
+int set_usol(gm_engine* e, const double* U, bool on_device, bool scaled = true) {
   if (!U) return fail(e, GM_ERR_ARG, "lanczos_create:badU: null U");
   const long long total = e->n * e->R;
   const double* src = U;
@@ -678,7 +678,8 @@ int set_usol(gm_engine* e, const double* U, bool on_device) {
     GM_CUDA(e, cudaMemcpyAsync(e->stage, U, total * sizeof(double), cudaMemcpyHostToDevice, e->stream));
     src = e->stage;
   }
-  k_pack_in<<<(unsigned)((total + 255) / 256), 256, 0, e->stream>>>(src, e->kp.Usol, e->n, e->R, e->col_scale);
+  k_pack_in<<<(unsigned)((total + 255) / 256), 256, 0, e->stream>>>(src, e->kp.Usol, e->n, e->R,
+                                                                   scaled ? e->col_scale : nullptr);
   GM_CUDA(e, cudaGetLastError());
   e->launches++;
   return GM_OK;
@@ -1245,6 +1246,25 @@ static int set_U_common(gm_handle h, const double* U, bool on_device) {
 }
 
 int gm_set_U(gm_handle h, const double* U_host) { return set_U_common(h, U_host, false); }
+
+int gm_get_ode(gm_handle h, double* ode_host) {
+  if (!h || !ode_host) return GM_ERR_ARG;
+  GM_CUDA(h, cudaMemcpyAsync(ode_host, h->kp.ode, (size_t)h->n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  return check_sync(h);
+}
+
+int gm_set_state(gm_handle h, const double* Usol_host, const double* ode_host) {
+  if (!h || !Usol_host) return GM_ERR_ARG;
+  if (ode_host)
+    GM_CUDA(h, cudaMemcpyAsync(h->kp.ode, ode_host, (size_t)h->n * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  int rc = set_usol(h, Usol_host, false, false);   // Usol as gm_get_U returned it: no column scaling
+  if (rc) return rc;
+  if (h->fe_cur == 0) h->fe_fwd_ok = false;
+  GM_CUDA(h, cudaMemsetAsync(h->kp.status, 0, sizeof(int), h->stream));
+  GM_CUDA(h, cudaMemsetAsync(h->kp.bar, 0, sizeof(unsigned), h->stream));
+  h->have_V = h->have_y = h->have_coef = false;
+  return launch(h, gm::PH_DEFLATE, 0);
+}
 
 int gm_set_U_device(gm_handle h, const double* U_dev) { return set_U_common(h, U_dev, true); }
 

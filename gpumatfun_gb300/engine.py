@@ -35,7 +35,7 @@ EXPORTED_SYMBOLS = [
     "gm_phase_times", "gm_info", "gm_get_meff", "gm_last_error", "gm_version",
     "gm_lin_sys_solves_noalloc", "gm_batch_create", "gm_time_loop", "gm_fe_attach", "gm_fe_assemble",
     "gm_fe_gradient", "gm_get_solution_device", "gm_fe_forward", "gm_fe_backward",
-    "gm_fe_backward_stored", "gm_get_basis",
+    "gm_fe_backward_stored", "gm_get_basis", "gm_get_ode", "gm_set_state",
 ]
 
 _dp = ct.POINTER(ct.c_double)
@@ -103,6 +103,8 @@ def load_library(build_if_missing: bool = False) -> ct.CDLL:
     for name in ("gm_get_U", "gm_get_xsol", "gm_get_aabb", "gm_get_update", "gm_get_solution", "gm_get_basis"):
         getattr(lib, name).argtypes = [h, _dp]
     lib.gm_set_U.argtypes = [h, _dp]
+    lib.gm_get_ode.argtypes = [h, _dp]
+    lib.gm_set_state.argtypes = [h, _dp, _dp]
     lib.gm_set_U_device.argtypes = [h, ct.c_void_p]
     lib.gm_set_y.argtypes = [h, _dp, _dp]
     lib.gm_get_y.argtypes = [h, _dp, _dp]
@@ -284,6 +286,22 @@ class Engine:
         out = np.empty(self.R * self.m * self.n)
         self._check(self._lib.gm_get_basis(self._h, _ptr(out)))
         return out.reshape(self.R, self.m, self.n)
+
+    def get_state(self):
+        """Checkpoint of a time loop: (Usol as get_U returns it, ode)."""
+        ode = np.empty(self.n)
+        self._check(self._lib.gm_get_ode(self._h, _ptr(ode)))
+        return self.get_U(), ode
+
+    def set_state(self, U, ode=None):
+        """Resume from get_state(): Usol without column scaling, and ode."""
+        u = _f64(np.asarray(U).reshape(self.n, -1).T).reshape(-1)
+        if u.size != self.n * self.R:
+            raise GmError(1, "set_state: U must be n x nrhs")
+        o = _f64(np.asarray(ode).reshape(-1)) if ode is not None else None
+        if o is not None and o.size != self.n:
+            raise GmError(1, "set_state: ode must have n entries")
+        self._check(self._lib.gm_set_state(self._h, _ptr(u), _ptr(o) if o is not None else None))
 
     def set_U(self, U):
         u = _f64(np.asarray(U).reshape(self.n, -1).T).reshape(-1)

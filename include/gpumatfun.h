@@ -228,6 +228,17 @@ int gm_get_basis(gm_handle h, double* dst);
 
 /* ---- additions with no reference counterpart ------------------------------ */
 
+/* Time-loop checkpoint and resume.  The state of a time loop after any step is
+ * Usol (gm_get_U: n x nrhs, column-major, with the column scaling applied)
+ * and the FitzHugh-Nagumo recovery variable ode (n; update_U_monodomain.cu
+ * keeps it on the device between steps).  gm_get_ode copies ode to the host;
+ * gm_set_state restores Usol exactly as gm_get_U returned it (no column
+ * scaling, unlike gm_set_U) and ode (NULL keeps the device copy),
+ * re-deflates and clears X, so the next steps continue the trajectory bit
+ * for bit. */
+int gm_get_ode(gm_handle h, double* ode_host);
+int gm_set_state(gm_handle h, const double* Usol_host, const double* ode_host);
+
 /* New right-hand sides (n x nrhs, column-major, host): U <- U_host o col_scale,
  * Usol = U, re-deflate, X = 0. */
 int gm_set_U(gm_handle h, const double* U_host);

@@ -59,3 +59,21 @@ def test_time_loop_graph_batch_of_many_blocks(engine_lib):
         a.time_loop(2, monodomain=True, graph=True)
     b.time_loop(6, monodomain=True, graph=False)
     np.testing.assert_array_equal(a.get_U(), b.get_U())
+
+
+@pytest.mark.parametrize("monodomain", [True, False])
+def test_checkpoint_resume_continues_bit_for_bit(engine_lib, monodomain):
+    """get_state after some steps, set_state on a fresh handle: the resumed
+    run continues the same trajectory bit for bit (Usol and the recovery
+    variable are the whole state of a time loop)."""
+    P, dt, ode, fhn = workloads.monodomain_problem(24, k=4, m=30, C=16)
+    a = make(P, dt, ode, fhn)
+    a.time_loop(5, monodomain=monodomain, graph=False)
+    U5, ode5 = a.get_state()
+    a.time_loop(4, monodomain=monodomain, graph=True)
+    b = make(P, dt, ode, fhn)
+    b.set_state(U5, ode5)
+    np.testing.assert_array_equal(b.get_U(), U5)
+    b.time_loop(4, monodomain=monodomain, graph=True)
+    np.testing.assert_array_equal(b.get_U(), a.get_U())
+    np.testing.assert_array_equal(b.get_state()[1], a.get_state()[1])
