@@ -2,6 +2,7 @@
 // conversion, device allocation, cooperative launches and the C ABI declared
 // in include/gpumatfun.h.
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <cmath>
@@ -608,7 +609,22 @@ int check_sync(gm_engine* e) {
 
 // Launch the persistent kernel with the given phases; slot selects the event
 // pair used for gm_phase_times.
+// NVTX range per engine phase (build_subspace, lin_sys_solves, apply_V,
+// deflate/update, fused solve), visible to Nsight tools and ncu --nvtx; a
+// no-op without a tool attached.
+struct PhaseRange {
+  explicit PhaseRange(int slot) {
+    static const char* const names[5] = {"gm:deflate_update", "gm:build_subspace", "gm:lin_sys_solves",
+                                         "gm:apply_V", "gm:solve"};
+    nvtxRangePushA(names[slot >= 0 && slot < 5 ? slot : 4]);
+  }
+  ~PhaseRange() { nvtxRangePop(); }
+  PhaseRange(const PhaseRange&) = delete;
+  PhaseRange& operator=(const PhaseRange&) = delete;
+};
+
 int launch(gm_engine* e, int phases, int slot) {
+  PhaseRange nvtx_range(slot);
   // The barrier counter returns to 0 after every completed barrier; it is
   // reset explicitly only after an aborted launch (gm_set_U clears errors).
   KParams kp = e->kp;
