@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--matrix-powers", type=int, default=None, choices=[0, 1],
                     help="1: two Horner levels of the polynomial per SpMV pass "
                          "(default: off for the f(A)b workloads, on for the adjoint)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batch-64: use the engine's default launch shape instead of the autotuned one")
     ap.add_argument("--unfused", action="store_true",
                     help="step = build_subspace + lin_sys_solves + apply_V (three launches) instead of gm_solve")
     ap.add_argument("--val-prefetch", type=int, default=0, choices=[0, 1, 2],
@@ -575,7 +577,7 @@ def run_batch(args):
     (one problem, one right-hand side per launch) on the same 256 solves.
     Plus the fractional monodomain time loop (512^2, 200 steps, CUDA graph)."""
     import torch
-    from gpumatfun_gb300 import BatchEngine, Engine, LanczosEngine, workloads
+    from gpumatfun_gb300 import BatchEngine, Engine, LanczosEngine, autotune, workloads
     K, W = args.steps, args.warmup
     t0 = time.perf_counter()
     probs = workloads.config5_batch()
@@ -583,8 +585,19 @@ def run_batch(args):
     nsolves = sum(P.R for P in probs)
     stream = torch.cuda.Stream()
     res, sols = {}, {}
+    shapes = {}
     for prec in ("mixed", "fp64"):
-        eng = BatchEngine(probs, precision=prec, sync=False)
+        shape = {}
+        if not args.no_autotune:
+            # row-block size, residency, staging and pass ordering tuned on this batch
+            t = autotune.tune_batch(probs, precision=prec, reps=2,
+                                    device=torch.cuda.get_device_name())
+            shape = {k: t[k] for k in ("threads", "blocks_per_sm", "col_staging", "sync_policy")}
+            default = [c for c in t.get("timed", []) if c["threads"] == 512 and c["blocks_per_sm"] == 0
+                       and c["col_staging"] == 0 and c["sync_policy"] == 0]
+            shapes[prec] = dict(shape, tuned_ms=t["ms"], default_shape_ms=default[0]["ms"] if default else None,
+                                cached=t["cached"], candidates=t["trials"])
+        eng = BatchEngine(probs, precision=prec, sync=False, **shape)
         ms = _timed_solves(eng, stream, K, W)
         sols[prec] = eng.split(eng.get_solution())
         res[prec] = {"ms_per_launch": ms, "solves_per_s": nsolves * 1e3 / ms, "grid_blocks": eng.info()["grid_blocks"],
@@ -646,6 +659,7 @@ def run_batch(args):
             "e2e": {"value": nsolves * 1e3 / e2e_ms, "unit": "solves/s", "h2d_bytes_per_step": 8 * n_total * probs[0].R,
                     "d2h_bytes_per_step": 8 * n_total * probs[0].R},
             "mixed_batched": res["mixed"], "fp64_batched": res["fp64"],
+            "launch_shape": shapes or "engine default (--no-autotune)",
             "fp64_single_solve": {"solves_per_s": single, "note": "each problem alone, 1 RHS per launch"},
             "mixed_batched_over_fp64_single": res["mixed"]["solves_per_s"] / single,
             "mixed_vs_fp64_rel_err": {"worst": max(errs), "median": float(np.median(errs))},

@@ -25,7 +25,8 @@ from typing import Callable
 
 import numpy as np
 
-__all__ = ["signature", "candidates", "tune", "default_cache_path"]
+__all__ = ["signature", "candidates", "tune", "default_cache_path", "batch_signature", "batch_candidates",
+           "tune_batch"]
 
 
 def default_cache_path() -> str:
@@ -78,14 +79,8 @@ def _measure_engine(P, precision: str, reps: int) -> Callable[[dict], float]:
     return run
 
 
-def tune(P, precision: str = "fp64", reps: int = 3, cache_path: str | None = None,
-         space: list | None = None, measure: Callable[[dict], float] | None = None,
-         device: str = "", force: bool = False) -> dict:
-    """Best launch shape for workload P: a dict of Engine keyword arguments
-    plus 'ms' (median fused-solve time).  ``measure`` replaces the GPU timing
-    (tests); ``space`` replaces the candidate list."""
-    cache_path = cache_path or default_cache_path()
-    key = signature(P, precision, device)
+def _search(key: str, space: list, measure: Callable[[dict], float], cache_path: str, force: bool) -> dict:
+    """Time every candidate (or reuse the cached winner for key) and cache the fastest."""
     cache = {}
     if os.path.exists(cache_path):
         try:
@@ -95,16 +90,15 @@ def tune(P, precision: str = "fp64", reps: int = 3, cache_path: str | None = Non
             cache = {}
     if not force and key in cache:
         return dict(cache[key], cached=True)
-    measure = measure or _measure_engine(P, precision, reps)
-    best, best_ms, trials = None, float("inf"), []
-    for cand in (space or candidates(P.R, P.d)):
+    best, best_ms, timed = None, float("inf"), []
+    for cand in space:
         ms = measure(cand)
-        trials.append(dict(cand, ms=ms))
+        timed.append(dict(cand, ms=ms))
         if ms < best_ms:
             best, best_ms = cand, ms
     if best is None:
         raise RuntimeError("autotune: no candidate ran")
-    result = dict(best, ms=best_ms, trials=len(trials))
+    result = dict(best, ms=best_ms, trials=len(timed), timed=timed)
     cache[key] = result
     os.makedirs(os.path.dirname(cache_path) or ".", exist_ok=True)
     tmp = f"{cache_path}.tmp{os.getpid()}"
@@ -112,3 +106,61 @@ def tune(P, precision: str = "fp64", reps: int = 3, cache_path: str | None = Non
         json.dump(cache, fh, indent=1)
     os.replace(tmp, cache_path)
     return dict(result, cached=False)
+
+
+def tune(P, precision: str = "fp64", reps: int = 3, cache_path: str | None = None,
+         space: list | None = None, measure: Callable[[dict], float] | None = None,
+         device: str = "", force: bool = False) -> dict:
+    """Best launch shape for workload P: a dict of Engine keyword arguments
+    plus 'ms' (median fused-solve time).  ``measure`` replaces the GPU timing
+    (tests); ``space`` replaces the candidate list."""
+    return _search(signature(P, precision, device), space or candidates(P.R, P.d),
+                   measure or _measure_engine(P, precision, reps), cache_path or default_cache_path(), force)
+
+
+def batch_signature(problems, precision: str, device: str = "") -> str:
+    """Key of a batch: every problem's n and nnz in order, plus the shared
+    nrhs, m, d, C and the precision."""
+    P0 = problems[0]
+    key = dict(sizes=[[int(P.n), int(P.A.nnz)] for P in problems], R=int(P0.R), m=int(P0.m), d=int(P0.d),
+               C=int(P0.C), precision=str(precision), device=device, batch=True)
+    return hashlib.sha1(json.dumps(key, sort_keys=True).encode()).hexdigest()[:16]
+
+
+def batch_candidates(R: int) -> list:
+    """Launch shapes of a batched engine: row-block size, residency, staging
+    and pass ordering (each problem keeps its own barrier)."""
+    bps = (0, 1) if R >= 4 else (0, 1, 2)
+    return [dict(threads=t, blocks_per_sm=b, col_staging=stg, sync_policy=pol)
+            for t, b, stg, pol in itertools.product((256, 512), bps, (0, 1), (0, 1))]
+
+
+def _measure_batch(problems, precision: str, reps: int) -> Callable[[dict], float]:
+    from .engine import BatchEngine, GmError
+
+    def run(cand: dict) -> float:
+        try:
+            eng = BatchEngine(problems, precision=precision, sync=False, **cand)
+        except GmError:
+            return float("inf")
+        try:
+            eng.solve()
+            eng.sync()
+            ts = []
+            for _ in range(reps):
+                eng.solve()
+                ts.append(eng.phase_times()["solve"])
+            return float(np.median(ts))
+        finally:
+            eng.delete()
+    return run
+
+
+def tune_batch(problems, precision: str = "mixed", reps: int = 3, cache_path: str | None = None,
+               space: list | None = None, measure: Callable[[dict], float] | None = None,
+               device: str = "", force: bool = False) -> dict:
+    """Best launch shape for a batch of problems in one engine: BatchEngine
+    keyword arguments plus 'ms' (median time of the one launch that solves all
+    of them)."""
+    return _search(batch_signature(problems, precision, device), space or batch_candidates(problems[0].R),
+                   measure or _measure_batch(problems, precision, reps), cache_path or default_cache_path(), force)

@@ -34,3 +34,23 @@ def test_matrix_powers_candidates_only_with_a_polynomial():
     assert all(c["matrix_powers"] == 0 for c in autotune.candidates(1, 0))
     mp = [c for c in autotune.candidates(1, 8) if c["matrix_powers"] == 1]
     assert mp and all(c["sync_policy"] == 0 for c in mp)
+
+
+def test_tune_batch_picks_fastest_and_caches(tmp_path):
+    probs = workloads.config5_batch(nprob=4, R=4, seed=1, lo=10, hi=20, m=8, C=8)
+    calls = []
+
+    def fake(c):
+        calls.append(c)
+        return 2.0 - (c["threads"] == 512) - 0.5 * (c["blocks_per_sm"] == 1) + 0.3 * c["sync_policy"]
+
+    path = tmp_path / "tune.json"
+    r = autotune.tune_batch(probs, "mixed", cache_path=str(path), measure=fake)
+    assert (r["threads"], r["blocks_per_sm"], r["sync_policy"]) == (512, 1, 0) and not r["cached"]
+    assert r["trials"] == len(autotune.batch_candidates(4)) == len(calls)
+    assert all(c["blocks_per_sm"] in (0, 1) for c in autotune.batch_candidates(4))
+    r2 = autotune.tune_batch(probs, "mixed", cache_path=str(path), measure=fake)
+    assert r2["cached"] and len(calls) == r["trials"]
+    # the batch key differs from any single problem's and from another batch's
+    assert autotune.batch_signature(probs, "mixed") != autotune.signature(probs[0], "mixed")
+    assert autotune.batch_signature(probs[:3], "mixed") != autotune.batch_signature(probs, "mixed")
