@@ -55,8 +55,10 @@ def parse():
     ap.add_argument("--matrix-powers", type=int, default=None, choices=[0, 1],
                     help="1: two Horner levels of the polynomial per SpMV pass "
                          "(default: off for the f(A)b workloads, on for the adjoint)")
-    ap.add_argument("--no-autotune", action="store_true",
-                    help="batch-64: use the engine's default launch shape instead of the autotuned one")
+    ap.add_argument("--autotune", default="auto", choices=["auto", "on", "off"],
+                    help="launch shape from the autotuner (auto: on for fd2d-* and batch-64, whose small "
+                         "problems gain from it; off for the large FE and 3D workloads, where sweeps found the "
+                         "engine default best)")
     ap.add_argument("--unfused", action="store_true",
                     help="step = build_subspace + lin_sys_solves + apply_V (three launches) instead of gm_solve")
     ap.add_argument("--val-prefetch", type=int, default=0, choices=[0, 1, 2],
@@ -204,6 +206,12 @@ def run_reference(args, P, rank):
     print(json.dumps(line), flush=True)
 
 
+def use_autotune(args) -> bool:
+    if args.autotune != "auto":
+        return args.autotune == "on"
+    return args.workload.startswith("fd2d-") or args.workload == "batch-64"
+
+
 def config_of(args, P):
     return {"workload": P.name, "n": int(P.n), "nnz": int(P.A.nnz), "m": int(P.m), "C": int(P.C),
             "d": int(P.d), "k": int(P.k), "nrhs": int(args.nrhs), "precision": args.precision,
@@ -221,11 +229,16 @@ def run_ours(args, P, rank, world, local):
     dev = torch.device("cuda", local)
     stream = torch.cuda.Stream(device=dev)
     R, K, W = args.nrhs, args.steps, args.warmup
+    shape = dict(threads=args.threads, blocks_per_sm=args.bps, col_staging=args.col_staging,
+                 matrix_powers=args.matrix_powers or 0)
+    tuned = None
+    if use_autotune(args):
+        from gpumatfun_gb300 import autotune
+        tuned = autotune.tune(P, args.precision, reps=3, device=torch.cuda.get_device_name(local))
+        shape = {k: tuned[k] for k in ("threads", "blocks_per_sm", "col_staging", "sync_policy", "matrix_powers")}
     eng = Engine.from_problem(P, precision=args.precision, sync=False, l2_window=args.l2_window,
-                              threads=args.threads, blocks_per_sm=args.bps,
-                              diag_compensation=args.diag_compensation, col_staging=args.col_staging,
-                              matrix_powers=args.matrix_powers or 0, max_blocks=args.max_blocks,
-                              reorth=args.reorth, val_prefetch=args.val_prefetch)
+                              diag_compensation=args.diag_compensation, max_blocks=args.max_blocks,
+                              reorth=args.reorth, val_prefetch=args.val_prefetch, **shape)
     eng.set_stream(stream.cuda_stream)
     n = P.n
     gen = torch.Generator(device=dev).manual_seed(1234 + rank)
@@ -335,6 +348,8 @@ def run_ours(args, P, rank, world, local):
             "roofline": roof, "clocks": clocks,
             "engine": {"grid_blocks": info["grid_blocks"], "threads": info["threads"],
                        "matrix_powers": info["matrix_powers"], "value_prefetch_bytes": info["value_prefetch_bytes"],
+                       "launch_shape": dict(shape, autotuned=tuned is not None,
+                                            cached=bool(tuned and tuned.get("cached"))),
                        "sell_padded": info["sell_padded"], "device_bytes": info["device_bytes"]}}
     eng.delete()
     del B
@@ -588,7 +603,7 @@ def run_batch(args):
     shapes = {}
     for prec in ("mixed", "fp64"):
         shape = {}
-        if not args.no_autotune:
+        if use_autotune(args):
             # row-block size, residency, staging and pass ordering tuned on this batch
             t = autotune.tune_batch(probs, precision=prec, reps=2,
                                     device=torch.cuda.get_device_name())
@@ -630,11 +645,17 @@ def run_batch(args):
     Pm, dt, ode, fhn = workloads.monodomain_problem(512)
     mono = {}
     Us = {}
+    mono_shapes = {}
     for prec in ("mixed", "fp64"):
+        mshape = {}
+        if use_autotune(args):
+            t = autotune.tune(Pm, prec, reps=2, device=torch.cuda.get_device_name())
+            mshape = {k: t[k] for k in ("threads", "blocks_per_sm", "col_staging", "sync_policy", "matrix_powers")}
+            mono_shapes[prec] = dict(mshape, tuned_ms=t["ms"])
         e = LanczosEngine(Pm.U, Pm.A, Pm.Q, Pm.lam, Pm.m, Pm.gamma, Pm.gs_re, Pm.gs_im, Pm.flam[:, 0],
                           Pm.flam[:, 1], dt, ode, fhn["aode"], fhn["bode"], fhn["code"], fhn["vrest"],
                           fhn["vamp"], fhn["vth"], fhn["vpeak"], fhn["c1ion"], fhn["c2ion"], np.ones(Pm.n),
-                          Pm.wts[0], Pm.wts[1], Pm.shifts, precision=prec, sync=False)
+                          Pm.wts[0], Pm.wts[1], Pm.shifts, precision=prec, sync=False, **mshape)
         e.set_stream(stream.cuda_stream)
         e.time_loop(200, monodomain=True, graph=True)   # capture + first replay
         Us[prec] = e.get_U()
@@ -665,7 +686,8 @@ def run_batch(args):
             "mixed_vs_fp64_rel_err": {"worst": max(errs), "median": float(np.median(errs))},
             "monodomain_512": {**{f"{p}_steps_per_s": mono[p]["steps_per_s"] for p in mono},
                                "steps": 200, "graph": True, "m": Pm.m, "C": Pm.C, "k": Pm.k,
-                               "mixed_vs_fp64_after_400_steps": mono_err},
+                               "mixed_vs_fp64_after_400_steps": mono_err,
+                               "launch_shape": mono_shapes or "engine default"},
             "setup_s": setup_s}
     print(json.dumps(line), flush=True)
 
