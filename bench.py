@@ -236,6 +236,7 @@ def run_ours(args, P, rank, world, local):
         from gpumatfun_gb300 import autotune
         tuned = autotune.tune(P, args.precision, reps=3, device=torch.cuda.get_device_name(local))
         shape = {k: tuned[k] for k in ("threads", "blocks_per_sm", "col_staging", "sync_policy", "matrix_powers")}
+        shape["sell_sigma"] = tuned.get("sell_sigma", 0)
     eng = Engine.from_problem(P, precision=args.precision, sync=False, l2_window=args.l2_window,
                               diag_compensation=args.diag_compensation, max_blocks=args.max_blocks,
                               reorth=args.reorth, val_prefetch=args.val_prefetch, **shape)
@@ -672,6 +673,7 @@ def run_batch(args):
         if use_autotune(args):
             t = autotune.tune(Pm, prec, reps=2, device=torch.cuda.get_device_name())
             mshape = {k: t[k] for k in ("threads", "blocks_per_sm", "col_staging", "sync_policy", "matrix_powers")}
+            mshape["sell_sigma"] = t.get("sell_sigma", 0)
             mono_shapes[prec] = dict(mshape, tuned_ms=t["ms"])
         e = LanczosEngine(Pm.U, Pm.A, Pm.Q, Pm.lam, Pm.m, Pm.gamma, Pm.gs_re, Pm.gs_im, Pm.flam[:, 0],
                           Pm.flam[:, 1], dt, ode, fhn["aode"], fhn["bode"], fhn["code"], fhn["vrest"],

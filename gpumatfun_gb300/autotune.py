@@ -6,7 +6,9 @@ keeps the fastest.  The knobs are the ones the engine exposes at create time:
 - resident blocks per SM;
 - TMA staging of SELL column indices on or off;
 - neighbour waits vs grid barriers between SpMV passes;
-- one or two Horner levels of the polynomial per SpMV pass (degree >= 2).
+- one or two Horner levels of the polynomial per SpMV pass (degree >= 2);
+- the SELL-32 sorting window sigma, for matrices whose row lengths vary
+  (sorting rows by length within a window cuts the slice padding).
 
 Results are cached in a JSON file keyed by a signature of the workload:
 - n, nnz, a row-length histogram and the number of right-hand sides;
@@ -44,18 +46,38 @@ def signature(P, precision: str, device: str = "") -> str:
     return hashlib.sha1(json.dumps(key, sort_keys=True).encode()).hexdigest()[:16]
 
 
-def candidates(R: int, degree: int = 0) -> list:
-    """The search space: row-block sizes, residency, staging, pass ordering
-    and, for a polynomial of degree >= 2, matrix-powers passes (neighbour
-    waits only)."""
+def candidates(R: int, degree: int = 0, ragged: bool = False) -> list:
+    """The search space: row-block sizes, residency, staging, pass ordering;
+    for a polynomial of degree >= 2, matrix-powers passes (neighbour waits
+    only, unsorted slices); for ragged row lengths, sigma-sorted slices."""
     threads = (128, 256, 512)
     bps = (0, 1) if R >= 4 else (0, 1, 2)
     out = []
     for t, b, stg, pol in itertools.product(threads, bps, (0, 1), (0, 1)):
-        out.append(dict(threads=t, blocks_per_sm=b, col_staging=stg, sync_policy=pol, matrix_powers=0))
+        out.append(dict(threads=t, blocks_per_sm=b, col_staging=stg, sync_policy=pol, matrix_powers=0, sell_sigma=0))
         if degree >= 2 and pol == 0:
-            out.append(dict(threads=t, blocks_per_sm=b, col_staging=stg, sync_policy=pol, matrix_powers=1))
+            out.append(dict(threads=t, blocks_per_sm=b, col_staging=stg, sync_policy=pol, matrix_powers=1,
+                            sell_sigma=0))
+        if ragged:
+            out.append(dict(threads=t, blocks_per_sm=b, col_staging=stg, sync_policy=pol, matrix_powers=0,
+                            sell_sigma=SIGMA))
     return out
+
+
+SIGMA = 256   # rows sorted by length within windows of 8 slices
+
+
+def ragged(P) -> bool:
+    """Row lengths vary enough that unsorted SELL-32 slices carry more than a
+    quarter of padding (each slice is as long as its longest row)."""
+    lens = np.diff(P.A.indptr)
+    n = lens.size
+    pad = np.zeros(-(-n // 32) * 32, dtype=np.int64)
+    pad[:n] = lens
+    per_slice = pad.reshape(-1, 32)
+    rows = np.minimum(32, n - 32 * np.arange(per_slice.shape[0]))
+    slots = int((per_slice.max(axis=1) * rows).sum())
+    return bool(slots > 1.25 * max(1, int(lens.sum())))
 
 
 def _measure_engine(P, precision: str, reps: int) -> Callable[[dict], float]:
@@ -114,7 +136,7 @@ def tune(P, precision: str = "fp64", reps: int = 3, cache_path: str | None = Non
     """Best launch shape for workload P: a dict of Engine keyword arguments
     plus 'ms' (median fused-solve time).  ``measure`` replaces the GPU timing
     (tests); ``space`` replaces the candidate list."""
-    return _search(signature(P, precision, device), space or candidates(P.R, P.d),
+    return _search(signature(P, precision, device), space or candidates(P.R, P.d, ragged(P)),
                    measure or _measure_engine(P, precision, reps), cache_path or default_cache_path(), force)
 
 

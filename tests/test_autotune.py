@@ -54,3 +54,23 @@ def test_tune_batch_picks_fastest_and_caches(tmp_path):
     # the batch key differs from any single problem's and from another batch's
     assert autotune.batch_signature(probs, "mixed") != autotune.signature(probs[0], "mixed")
     assert autotune.batch_signature(probs[:3], "mixed") != autotune.batch_signature(probs, "mixed")
+
+
+def test_sigma_candidates_only_for_ragged_rows():
+    import numpy as np
+    import scipy.sparse as sp
+    P = workloads.config1_small(N=12, k=2, m=10, C=8, R=1)
+    assert not autotune.ragged(P)                       # 5-point stencil: uniform rows
+    assert all(c["sell_sigma"] == 0 for c in autotune.candidates(1, 0, autotune.ragged(P)))
+    # one dense row in every 32 makes SELL-32 slices mostly padding
+    n = 256
+    rows, cols = [np.arange(n)], [np.arange(n)]
+    for r in range(0, n, 32):
+        rows.append(np.full(64, r)); cols.append(np.arange(64))
+    A = sp.csr_matrix((np.ones(sum(len(x) for x in rows)), (np.concatenate(rows), np.concatenate(cols))),
+                      shape=(n, n))
+    Q = workloads.make_problem("ragged", A + A.T, np.ones((n, 1)), np.zeros((n, 0)), np.zeros(0),
+                               P.funcs[:1], 8, 8, 0.5, 200.0)
+    assert autotune.ragged(Q)
+    sig = [c for c in autotune.candidates(1, 4, True) if c["sell_sigma"]]
+    assert sig and all(c["matrix_powers"] == 0 for c in sig)
