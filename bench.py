@@ -151,6 +151,27 @@ def profiled_traffic(workload: str, precision: str, nrhs: int):
     return None
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    import platform
+    import subprocess
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.strip().lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as fh:
+            for line in fh:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.machine()
+
+
 def cpu_sample(P, U_defl, budget_s: float, threads: int):
     """Time the reference CPU algorithm on the host (bounded sample)."""
     from oracle import cpu_fab
@@ -163,7 +184,8 @@ def cpu_sample(P, U_defl, budget_s: float, threads: int):
         cpu_fab.run(P.A, U_defl[:, :1], P.m, P.gamma, P.gs_re, P.gs_im, P.wts[:1], P.sigma, threads=th)
         reps += 1
     dt = (time.perf_counter() - t0) / reps
-    return dict(value=1.0 / dt, unit="solves/s", cores=int(th), kind="port",
+    return dict(value=1.0 / dt, unit="solves/s", cores=int(th), kind="port", cpu_model=cpu_model(),
+                host_cpus=os.cpu_count(),
                 sample=f"{reps} full f(A)b solve(s) of 1 RHS (n={P.n}, m={P.m}, d={P.d}, C={P.C}) "
                        f"by the C/OpenMP restatement of nicksmethodcpu.m; {dt:.3f} s each")
 
@@ -200,6 +222,7 @@ def run_reference(args, P, rank):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": config_of(args, P),
             "cpu_baseline": {"value": v, "unit": "solves/s", "cores": th, "kind": "port",
+                             "cpu_model": cpu_model(), "host_cpus": os.cpu_count(),
                              "sample": f"{steps} full f(A)b solve(s) of 1 RHS by the C/OpenMP restatement of "
                                        "nicksmethodcpu.m (MATLAB CPU path); host-side deflation excluded"},
             "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
