@@ -54,7 +54,8 @@ def test_create_rejects_bad_arguments_before_device(engine_lib):
                 wts=g.ctypes.data_as(E._dp), shifts=g.ctypes.data_as(E._dp))
     cases = [(dict(nrhs=3), "nrhs"), (dict(struct_version=7), "struct_version"), (dict(n=0), "inputNotSquare"),
              (dict(subspace_size=0), "bad_N"), (dict(gamma_size=0), "bad_gamma"), (dict(precision=5), "precision"),
-             (dict(num_eigs=2), "badQ"), (dict(format=9), "format")]
+             (dict(num_eigs=2), "badQ"), (dict(format=9), "format"), (dict(reorth=3), "reorth"),
+             (dict(reorth=-1), "reorth")]
     for over, msg in cases:
         kw = dict(base)
         kw.update(over)
