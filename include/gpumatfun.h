@@ -121,9 +121,8 @@ typedef struct gm_create_args {
                                   near-null vector: ones for a graph Laplacian,
                                   M^{1/2} 1 for M^{-1/2} K M^{-1/2}); NULL = ones  */
   int diag_compensation;       /* mixed engine: 0 = on (default), 1 = off          */
-  int max_blocks;              /* > 0: at most this many blocks in the grid (fewer
-                                  blocks make every barrier cheaper on problems
-                                  too small to fill the GPU); 0 = engine default */
+  int max_blocks;              /* > 0: at most this many blocks in the grid
+                                  (a tuning knob); 0 = engine default            */
   int matrix_powers;           /* 1 = two Horner levels of the polynomial per SpMV
                                   pass (halo rows recomputed per block, the level
                                   in between in shared memory), where it applies:
