@@ -19,6 +19,8 @@
 //   aabb         (m+1) x 2R column-major: alpha_r in column r, beta_r in R+r
 //   Yr, Yi       m x (R C) column-major (column r*C + j), as the reference
 //   coef         [R][d+1][m] FP64, coef_ff the float-float copy
+//   hpart, hblk  (Gram-Schmidt only) per-block partial dots [2][m+8][R][G]
+//                and each block's totals [G][m+1][R]
 #pragma once
 #include "fab_common.cuh"
 
