@@ -11,7 +11,6 @@ missing library raises immediately.
 from __future__ import annotations
 
 import ctypes as ct
-from pathlib import Path
 from typing import Sequence
 
 import numpy as np

@@ -14,7 +14,7 @@ import ctypes as ct
 import numpy as np
 import pytest
 
-from gpumatfun_gb300 import Engine, engine as E, workloads
+from gpumatfun_gb300 import Engine, workloads
 
 pytestmark = pytest.mark.gpu
 
