@@ -44,6 +44,8 @@ def parse():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true", help="skip the mixed/batched and oracle checks")
+    ap.add_argument("--no-config-extras", action="store_true",
+                    help="skip the 256^3, batch-64 and adjoint-250k fields of the default line")
     ap.add_argument("--cpu-sample-s", type=float, default=30.0)
     ap.add_argument("--threads", type=int, default=0, help="threads per block (0: engine default)")
     ap.add_argument("--bps", type=int, default=0, help="resident blocks per SM (0: engine default)")
@@ -353,6 +355,11 @@ def run_ours(args, P, rank, world, local):
             "peak_kind": f"{peak_kind} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
             else "fallback 6.8 TB/s", "traffic": traffic, "algorithmic_bytes_per_launch": alg,
             "ms_per_launch": ms_fused,
+            "frac_kind": "effective: algorithmic bytes over the launch time; the SELL matrix is served from "
+                         "the L2 persisting window on every pass after the first, so DRAM moves fewer bytes "
+                         "(dram_frac)",
+            "dram_achieved": traffic / (ms_fused * 1e-3) / 1e9 if traffic else None,
+            "dram_frac": traffic / (ms_fused * 1e-3) / 1e9 / peak if traffic else None,
             "fp64_tflops": roofline.fused_solve_flops(sizes) / (ms_fused * 1e-3) / 1e12}
     if args.precision == "fp64":
         # the FP64 pipe is the binding unit on GB300 (2 FMA lanes per clock per
@@ -385,6 +392,21 @@ def run_ours(args, P, rank, world, local):
             line["mixed_batched"] = mixed_batched(P, K, W, dev, stream, x_ref_engine=None)
             if args.reorth == 0:
                 line["reorth_cgs"] = reorth_extra(P, K, W, stream)
+    if rank == 0 and not args.no_extras and not args.no_config_extras and P.name.startswith("fe-disk-1M"):
+        # the other configurations of the metric, measured in the same run:
+        # 256^3 mixed and FP64 (the largest single-GPU configuration), the
+        # 64-problem batch against the plain FP64 single-solve engine, and the
+        # 250k-node adjoint with its finite-difference checks
+        ke, we = max(3, min(K, 10)), max(3, min(W, 3))
+        line["fd3d_256"] = _extra("fd3d_256", fd3d_measure, 256, ke, we)
+        line["batch_64"] = _extra("batch_64", batch_measure, ke, we, tune=False, monodomain=False)
+        if "mixed_batched_over_fp64_single" in line["batch_64"]:
+            line["mixed_batched_over_plain_fp64"] = {
+                "batch_64": line["batch_64"]["mixed_batched_over_fp64_single"],
+                "fe_disk_1M_R4": line.get("mixed_batched", {}).get("mixed_solves_per_s", 0.0) / (R * 1e3 / ms_fused),
+                "note": "mixed engine, 4 right-hand sides per launch, over the plain FP64 engine with one "
+                        "right-hand side per launch; fused launches on both sides"}
+        line["adjoint_250k"] = _extra("adjoint_250k", adjoint_measure, 250_000, 3, 2)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(P, host_deflate(P, P.U), args.cpu_sample_s, 0)
     if rank == 0:
@@ -487,22 +509,24 @@ def mixed_batched(P, K, W, dev, stream, x_ref_engine=None):
             "note": "fused launch only (b resident, deflation excluded); same b for both precisions"}
 
 
-def run_adjoint(args):
-    """Adjoint workload: x = f(A(kappa)) b on the 250k-node FE disk, loss
-    L = 1/2 ||x - d||^2, one step = forward + backward (dL/dkappa per
-    triangle and dL/db) through the same calls torch.autograd uses (the
-    backward reuses the forward's stored Krylov state)."""
+def adjoint_measure(n_target: int, K: int, W: int, matrix_powers=None, fd_directions: int = 64) -> dict:
+    """Adjoint workload: x = f(A(kappa)) b on the FE disk with ``n_target``
+    nodes, loss L = 1/2 ||x - d||^2, one step = forward + backward
+    (dL/dkappa per triangle and dL/db) through the same calls
+    torch.autograd uses (the backward reuses the forward's stored Krylov
+    state), in FP64 and with FP32 storage; then central finite differences of
+    the loss on random directions (the configured check: white-noise
+    directions v = kappa * N(0, 1) at step 1e-6, beside step 1e-3 and smooth
+    Gaussian-field directions), in both precisions."""
     import torch
     from gpumatfun_gb300 import adjoint, workloads
-    n_target = int(args.workload.split("-")[-1].replace("k", "000"))
-    K, W = args.steps, args.warmup
     t0 = time.perf_counter()
     mesh, kappa, kstar, b = workloads.adjoint_case(n_target)
     prm = dict(workloads.ADJOINT_PARAMS)
     out = {}
     ops = {}
     for prec in ("fp64", "mixed"):
-        mp = 1 if args.matrix_powers is None else args.matrix_powers
+        mp = 1 if matrix_powers is None else matrix_powers
         ops[prec] = adjoint.FracFEOperator(mesh, kappa, precision=prec, matrix_powers=mp, **prm)
     setup_s = time.perf_counter() - t0
     op = ops["fp64"]
@@ -531,7 +555,7 @@ def run_adjoint(args):
             torch.cuda.synchronize()
             tf += e[0].elapsed_time(e[1])
             tb += e[1].elapsed_time(e[2])
-        grads[prec] = (dk.cpu().numpy(), db.cpu().numpy(), x.cpu().numpy())
+        grads[prec] = (dk.clone(), db.cpu().numpy(), x.cpu().numpy())
         out[prec] = {"grad_evals_per_s": 1e3 * K / (tf + tb), "forward_ms": tf / K, "backward_ms": tb / K}
     # end to end with host buffers (numpy in, numpy out), FP64
     kh, bh = np.ascontiguousarray(kappa), np.ascontiguousarray(b)
@@ -550,71 +574,82 @@ def run_adjoint(args):
     dk64, db64, x64 = grads["fp64"]
     dkm, dbm, xm = grads["mixed"]
     rel = lambda a, r: float(np.linalg.norm(a - r) / np.linalg.norm(r))
-    # central finite differences of the FP64 loss on 64 random directions
-    # v = kappa * N(0, 1) per triangle, at the step 1e-6 and at 1e-3; the
-    # rounding noise of the loss itself is measured by perturbing kappa by
-    # 1e-14 relative, and bounds what the small step can resolve (noise / h).
-    def loss(k):
-        xx = op.forward(k, bt)
-        return 0.5 * float(torch.sum((xx - d) ** 2))
-    dkt = torch.as_tensor(dk64, device=dev)
-    L0 = loss(kt)
-    noise = max(abs(loss(kt * (1 + 1e-14 * torch.randn(kt.shape, generator=gen, device=dev,
-                                                            dtype=torch.float64))) - L0) for _ in range(3))
-    dirs = [kt * torch.randn(kt.shape, generator=gen, device=dev, dtype=torch.float64) for _ in range(64)]
-    ads = np.array([float(torch.dot(dkt, v)) for v in dirs])
-    t2 = time.perf_counter()
-    fd_out = {}
-    for h in (1e-6, 1e-3):
-        fds = np.array([(loss(kt + h * v) - loss(kt - h * v)) / (2 * h) for v in dirs])
-        err = np.abs(fds - ads) / np.sqrt(np.mean(ads ** 2))
-        fd_out[f"h={h:g}"] = {"max_err": float(err.max()), "median_err": float(np.median(err)),
-                              "noise_bound": float(noise / h / np.sqrt(np.mean(ads ** 2)))}
-    # smooth random directions: v = kappa * g with g a Gaussian random field
-    # (sigma 1, correlation length 0.1, as the coefficient's own field) at the
-    # triangle centroids; their directional derivatives are large against the
-    # loss's rounding noise, so FD resolves them at the larger step, where
-    # Richardson extrapolation of steps h and h/2 removes the h^2 term
+
+    # Central finite differences of the loss.  The rounding noise of the loss
+    # itself is measured by perturbing kappa by 1e-14 relative; noise / h
+    # bounds what a step h can resolve.
     from gpumatfun_gb300 import problems as _pb
     cent = mesh.nodes[mesh.tris].mean(axis=1)
-    sdirs = [kt * torch.as_tensor(_pb.gaussian_random_field(cent, sigma=1.0, ell=0.1, seed=1000 + s), device=dev)
-             for s in range(64)]
-    sads = np.array([float(torch.dot(dkt, v)) for v in sdirs])
-    h = 1e-3
-    c1 = np.array([(loss(kt + h * v) - loss(kt - h * v)) / (2 * h) for v in sdirs])
-    c2 = np.array([(loss(kt + 0.5 * h * v) - loss(kt - 0.5 * h * v)) / h for v in sdirs])
-    rich = (4 * c2 - c1) / 3
-    srms = np.sqrt(np.mean(sads ** 2))
-    fd_out["smooth_directions"] = {
-        "h=0.001": {"max_err": float((np.abs(c1 - sads) / srms).max()),
-                    "median_err": float(np.median(np.abs(c1 - sads) / srms))},
-        "richardson h=0.001,0.0005": {"max_err": float((np.abs(rich - sads) / srms).max()),
-                                      "median_err": float(np.median(np.abs(rich - sads) / srms))},
-        "noise_bound": float(3 * noise / h / srms), "rms_directional_derivative": float(srms)}
-    fd_out.update({"directions": 64, "loss": L0, "loss_noise": noise,
-                   "err": "|FD - adjoint| / rms(adjoint) over the directions; noise_bound = loss_noise / h "
-                          "in the same units", "seconds": time.perf_counter() - t2})
+    t2 = time.perf_counter()
+    fd_out = {"directions": fd_directions,
+              "err": "|FD - adjoint| / rms(adjoint) over the directions; noise_bound = loss noise / h "
+                     "in the same units"}
+    for prec, o in ops.items():
+        dkt = grads[prec][0]
+
+        def loss(k):
+            xx = o.forward(k, bt)
+            return 0.5 * float(torch.sum((xx - d) ** 2))
+        L0 = loss(kt)
+        lnoise = max(abs(loss(kt * (1 + 1e-14 * torch.randn(kt.shape, generator=gen, device=dev,
+                                                               dtype=torch.float64))) - L0) for _ in range(3))
+        # the configured check: white-noise directions, step 1e-6 (and 1e-3)
+        dirs = [kt * torch.randn(kt.shape, generator=gen, device=dev, dtype=torch.float64)
+                for _ in range(fd_directions)]
+        ads = np.array([float(torch.dot(dkt, v)) for v in dirs])
+        rms = float(np.sqrt(np.mean(ads ** 2)))
+        res = {"loss": L0, "loss_noise": lnoise}
+        for h in (1e-6, 1e-3):
+            fds = np.array([(loss(kt + h * v) - loss(kt - h * v)) / (2 * h) for v in dirs])
+            err = np.abs(fds - ads) / rms
+            res[f"white_h={h:g}"] = {"max_err": float(err.max()), "median_err": float(np.median(err)),
+                                     "noise_bound": float(lnoise / h / rms)}
+        # smooth directions v = kappa * g, g a Gaussian random field (sigma 1,
+        # correlation length 0.1) at the triangle centroids: directional
+        # derivatives large against the loss noise
+        sdirs = [kt * torch.as_tensor(_pb.gaussian_random_field(cent, sigma=1.0, ell=0.1, seed=1000 + s),
+                                      device=dev) for s in range(fd_directions)]
+        sads = np.array([float(torch.dot(dkt, v)) for v in sdirs])
+        srms = float(np.sqrt(np.mean(sads ** 2)))
+        h = 1e-3
+        c1 = np.array([(loss(kt + h * v) - loss(kt - h * v)) / (2 * h) for v in sdirs])
+        serr = np.abs(c1 - sads) / srms
+        res["smooth_h=0.001"] = {"max_err": float(serr.max()), "median_err": float(np.median(serr)),
+                                 "noise_bound": float(lnoise / h / srms), "rms_directional_derivative": srms}
+        fd_out[prec] = res
+    fd_out["seconds"] = time.perf_counter() - t2
+    res = {"config": {"n": int(op.n), "ntri": int(op.ntri), **prm, "l1": op.l1, "lN": op.lN,
+                      "matrix_powers": int(op.engine.info()["matrix_powers"])},
+           "fp64": out["fp64"], "mixed": out["mixed"],
+           "e2e_grad_evals_per_s": 1.0 / e2e_s,
+           "e2e_bytes": {"h2d_bytes_per_step": 8 * (2 * op.ntri + 3 * op.n), "d2h_bytes_per_step": 8 * (op.ntri + 2 * op.n)},
+           "mixed_vs_fp64": {"x": rel(xm, x64), "dL_dkappa": rel(dkm.cpu().numpy(), dk64.cpu().numpy()),
+                             "dL_db": rel(dbm, db64)},
+           "finite_differences": fd_out, "setup_s": setup_s}
+    for o in ops.values():
+        o.delete()
+    return res
+
+
+def run_adjoint(args):
+    """The adjoint workload's own JSON line (``--workload fe-adjoint-<n>k``)."""
+    n_target = int(args.workload.split("-")[-1].replace("k", "000"))
+    K, W = args.steps, args.warmup
+    r = adjoint_measure(n_target, K, W, matrix_powers=args.matrix_powers)
     line = {"metric": "adjoint gradient evaluations/s (forward + backward: dL/dkappa per triangle and dL/db)",
-            "value": out["fp64"]["grad_evals_per_s"], "unit": "grad-evals/s", "n_gpus": 1, "steps": K, "warmup": W,
-            "ms_per_step": out["fp64"]["forward_ms"] + out["fp64"]["backward_ms"], "higher_is_better": True,
+            "value": r["fp64"]["grad_evals_per_s"], "unit": "grad-evals/s", "n_gpus": 1, "steps": K, "warmup": W,
+            "ms_per_step": r["fp64"]["forward_ms"] + r["fp64"]["backward_ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded disk mesh, two Gaussian-field coefficients kappa and kappa*, uniform b, "
                     "d = f(A(kappa*)) b + 1% noise)",
-            "config": {"workload": args.workload, "n": int(op.n), "ntri": int(op.ntri), **prm,
-                       "l1": op.l1, "lN": op.lN, "matrix_powers": int(op.engine.info()["matrix_powers"])},
-            "e2e": {"value": 1.0 / e2e_s, "unit": "grad-evals/s", "h2d_bytes_per_step": 8 * (2 * op.ntri + 3 * op.n),
-                    "d2h_bytes_per_step": 8 * (op.ntri + 2 * op.n)},
-            "fp64": out["fp64"], "mixed": out["mixed"],
-            "mixed_vs_fp64": {"x": rel(xm, x64), "dL_dkappa": rel(dkm, dk64), "dL_db": rel(dbm, db64)},
-            "finite_differences": fd_out,
-            "setup_s": setup_s}
-    for o in ops.values():
-        o.delete()
+            "config": {"workload": args.workload, **r["config"]},
+            "e2e": {"value": r["e2e_grad_evals_per_s"], "unit": "grad-evals/s", **r["e2e_bytes"]},
+            **{k: r[k] for k in ("fp64", "mixed", "mixed_vs_fp64", "finite_differences", "setup_s")}}
     print(json.dumps(line), flush=True)
 
 
 def _timed_solves(eng, stream, K, W):
-    """Median-free device time of K back-to-back fused solves on ``stream`` (ms per solve)."""
+    """Device time of K back-to-back fused solves on ``stream`` (ms per solve)."""
     import torch
     eng.set_stream(stream.cuda_stream)
     with torch.cuda.stream(stream):
@@ -630,15 +665,21 @@ def _timed_solves(eng, stream, K, W):
     return e0.elapsed_time(e1) / K
 
 
-def run_batch(args):
+# Launch shape of the batch when it is not autotuned: the one the autotuner
+# chose on GB300 for both precisions (256-thread blocks, grid barriers
+# between passes, column staging on, residency from the occupancy limit).
+BATCH_SHAPE = dict(threads=256, blocks_per_sm=0, col_staging=0, sync_policy=1)
+
+
+def batch_measure(K: int, W: int, tune: bool, monodomain: bool = True) -> dict:
     """Batched serving-style workload: 64 fractional-diffusion problems of
     uneven size (N^2 grids, N log-uniform in [64, 1024]), 4 right-hand sides
-    each, one persistent launch; against the plain FP64 single-solve engine
-    (one problem, one right-hand side per launch) on the same 256 solves.
-    Plus the fractional monodomain time loop (512^2, 200 steps, CUDA graph)."""
+    each, one persistent launch, in both precisions; against the plain FP64
+    single-solve engine (one problem, one right-hand side per launch) on the
+    same 256 solves.  Optionally the fractional monodomain time loop (512^2,
+    200 steps, CUDA graph)."""
     import torch
     from gpumatfun_gb300 import BatchEngine, Engine, LanczosEngine, autotune, workloads
-    K, W = args.steps, args.warmup
     t0 = time.perf_counter()
     probs = workloads.config5_batch()
     setup_s = time.perf_counter() - t0
@@ -646,17 +687,19 @@ def run_batch(args):
     stream = torch.cuda.Stream()
     res, sols = {}, {}
     shapes = {}
+    e2e_ms = n_total = None
     for prec in ("mixed", "fp64"):
-        shape = {}
-        if use_autotune(args):
+        shape = dict(BATCH_SHAPE)
+        if tune:
             # row-block size, residency, staging and pass ordering tuned on this batch
-            t = autotune.tune_batch(probs, precision=prec, reps=2,
-                                    device=torch.cuda.get_device_name())
+            t = autotune.tune_batch(probs, precision=prec, reps=2, device=torch.cuda.get_device_name())
             shape = {k: t[k] for k in ("threads", "blocks_per_sm", "col_staging", "sync_policy")}
             default = [c for c in t.get("timed", []) if c["threads"] == 512 and c["blocks_per_sm"] == 0
                        and c["col_staging"] == 0 and c["sync_policy"] == 0]
             shapes[prec] = dict(shape, tuned_ms=t["ms"], default_shape_ms=default[0]["ms"] if default else None,
                                 cached=t["cached"], candidates=t["trials"])
+        else:
+            shapes[prec] = dict(shape, autotuned=False)
         eng = BatchEngine(probs, precision=prec, sync=False, **shape)
         ms = _timed_solves(eng, stream, K, W)
         sols[prec] = eng.split(eng.get_solution())
@@ -686,6 +729,20 @@ def run_batch(args):
         single_ms += P.R * _timed_solves(e, stream, max(2, K // 2), 1)
         e.delete()
     single = nsolves * 1e3 / single_ms
+    sizes = [int(P.meta["N"]) for P in probs]
+    out = {"config": {"workload": "batch-64", "problems": len(probs), "nrhs": probs[0].R,
+                      "grid_N": [min(sizes), max(sizes)], "rows_total": int(sum(P.n for P in probs)),
+                      "m": probs[0].m, "C": probs[0].C,
+                      "f": "exp(-dt K_alpha lambda^0.75), dt 0.05, K_alpha 1e-4, side 2.5"},
+           "mixed_batched": res["mixed"], "fp64_batched": res["fp64"], "launch_shape": shapes,
+           "fp64_single_solve": {"solves_per_s": single, "note": "each problem alone, 1 RHS per launch"},
+           "mixed_batched_over_fp64_single": res["mixed"]["solves_per_s"] / single,
+           "mixed_vs_fp64_rel_err": {"worst": max(errs), "median": float(np.median(errs))},
+           "e2e_solves_per_s": nsolves * 1e3 / e2e_ms,
+           "e2e_bytes": {"h2d_bytes_per_step": 8 * n_total * probs[0].R, "d2h_bytes_per_step": 8 * n_total * probs[0].R},
+           "setup_s": setup_s}
+    if not monodomain:
+        return out
     # fractional monodomain time loop, CUDA graph of 200 steps
     Pm, dt, ode, fhn = workloads.monodomain_problem(512)
     mono = {}
@@ -693,7 +750,7 @@ def run_batch(args):
     mono_shapes = {}
     for prec in ("mixed", "fp64"):
         mshape = {}
-        if use_autotune(args):
+        if tune:
             t = autotune.tune(Pm, prec, reps=2, device=torch.cuda.get_device_name())
             mshape = {k: t[k] for k in ("threads", "blocks_per_sm", "col_staging", "sync_policy", "matrix_powers")}
             mshape["sell_sigma"] = t.get("sell_sigma", 0)
@@ -714,28 +771,78 @@ def run_batch(args):
         mono[prec] = {"steps_per_s": 200e3 / e0.elapsed_time(e1), "ms_per_step": e0.elapsed_time(e1) / 200}
         e.delete()
     mono_err = float(np.linalg.norm(Us["mixed"][:, 0] - Us["fp64"][:, 0]) / np.linalg.norm(Us["fp64"][:, 0]))
-    sizes = [int(P.meta["N"]) for P in probs]
+    out["monodomain_512"] = {**{f"{p}_steps_per_s": mono[p]["steps_per_s"] for p in mono},
+                             "steps": 200, "graph": True, "m": Pm.m, "C": Pm.C, "k": Pm.k,
+                             "mixed_vs_fp64_after_200_steps": mono_err,
+                             "launch_shape": mono_shapes or "engine default"}
+    return out
+
+
+def run_batch(args):
+    """The batched workload's own JSON line (``--workload batch-64``)."""
+    K, W = args.steps, args.warmup
+    r = batch_measure(K, W, tune=use_autotune(args), monodomain=True)
     line = {"metric": "batched f(A)b solves/s (64 uneven fractional-diffusion problems x 4 RHS, one launch)",
-            "value": res["mixed"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": K, "warmup": W,
-            "ms_per_step": res["mixed"]["ms_per_launch"], "higher_is_better": True, "scaling": "weak",
+            "value": r["mixed_batched"]["solves_per_s"], "unit": "solves/s", "n_gpus": 1, "steps": K, "warmup": W,
+            "ms_per_step": r["mixed_batched"]["ms_per_launch"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32-storage/f64-recurrence",
-            "data": "synthetic (seeded grid sizes and right-hand sides)",
-            "config": {"workload": "batch-64", "problems": len(probs), "nrhs": probs[0].R, "grid_N": [min(sizes), max(sizes)],
-                       "rows_total": int(sum(P.n for P in probs)), "m": probs[0].m, "C": probs[0].C,
-                       "f": "exp(-dt K_alpha lambda^0.75), dt 0.05, K_alpha 1e-4, side 2.5"},
-            "e2e": {"value": nsolves * 1e3 / e2e_ms, "unit": "solves/s", "h2d_bytes_per_step": 8 * n_total * probs[0].R,
-                    "d2h_bytes_per_step": 8 * n_total * probs[0].R},
-            "mixed_batched": res["mixed"], "fp64_batched": res["fp64"],
-            "launch_shape": shapes or "engine default (--no-autotune)",
-            "fp64_single_solve": {"solves_per_s": single, "note": "each problem alone, 1 RHS per launch"},
-            "mixed_batched_over_fp64_single": res["mixed"]["solves_per_s"] / single,
-            "mixed_vs_fp64_rel_err": {"worst": max(errs), "median": float(np.median(errs))},
-            "monodomain_512": {**{f"{p}_steps_per_s": mono[p]["steps_per_s"] for p in mono},
-                               "steps": 200, "graph": True, "m": Pm.m, "C": Pm.C, "k": Pm.k,
-                               "mixed_vs_fp64_after_400_steps": mono_err,
-                               "launch_shape": mono_shapes or "engine default"},
-            "setup_s": setup_s}
+            "data": "synthetic (seeded grid sizes and right-hand sides)", "config": r["config"],
+            "e2e": {"value": r["e2e_solves_per_s"], "unit": "solves/s", **r["e2e_bytes"]},
+            **{k: v for k, v in r.items() if k not in ("config", "e2e_solves_per_s", "e2e_bytes")}}
     print(json.dumps(line), flush=True)
+
+
+def fd3d_measure(N: int, K: int, W: int) -> dict:
+    """Config 3 (3D 7-point variable-coefficient Laplacian on N^3, m = 100,
+    f = exp(-5e-4 lambda^0.6)) in both precisions: fused-launch solves/s,
+    algorithmic GB/s and its fraction of the measured HBM peak (the 1.4 GB
+    FP32 / 2.3 GB FP64 matrix is streamed from HBM every pass, so this is a
+    DRAM-level figure), the DRAM traffic of the committed ncu summary, and
+    the mixed result's error against the FP64 engine on the same b."""
+    import torch
+    from gpumatfun_gb300 import Engine, roofline, workloads
+    t0 = time.perf_counter()
+    P = workloads.config3(N=N)
+    setup_s = time.perf_counter() - t0
+    stream = torch.cuda.Stream()
+    peak, _ = measured_peaks()
+    out = {"config": {"workload": f"fd3d-{N}", "n": int(P.n), "nnz": int(P.A.nnz), "m": P.m, "C": P.C, "d": P.d,
+                      "k": P.k, "nrhs": 1, "f": "exp(-5e-4 x^0.6)"}}
+    xs = {}
+    for prec in ("mixed", "fp64"):
+        eng = Engine.from_problem(P, precision=prec, sync=False)
+        ms = _timed_solves(eng, stream, K, W)
+        xs[prec] = eng.get_solution()
+        info = eng.info()
+        eng.delete()
+        sz = roofline.Sizes(n=P.n, nnz=int(P.A.nnz), R=1, m=P.m, d=P.d, C=P.C, k=P.k, mixed=prec == "mixed")
+        alg = roofline.fused_solve_bytes(sz)
+        ach = alg / (ms * 1e-3) / 1e9
+        traffic = profiled_traffic(f"fd3d-{N}", prec, 1)
+        out[prec] = {"solves_per_s": 1e3 / ms, "ms_per_launch": ms, "algorithmic_bytes_per_launch": alg,
+                     "achieved_gb_s": ach, "peak_gb_s": peak, "frac": ach / peak,
+                     "traffic": traffic,
+                     "dram_frac": (traffic / (ms * 1e-3) / 1e9 / peak) if traffic else None,
+                     "grid_blocks": info["grid_blocks"], "value_prefetch_bytes": info["value_prefetch_bytes"]}
+    out["mixed_rel_err_vs_fp64_engine"] = float(np.linalg.norm(xs["mixed"] - xs["fp64"]) / np.linalg.norm(xs["fp64"]))
+    out["mixed_over_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
+    out["setup_s"] = setup_s
+    return out
+
+
+def _extra(name, fn, *a, **kw):
+    """Run one extra measurement; a failure is recorded in the line instead of
+    ending the run."""
+    import torch
+    t0 = time.perf_counter()
+    try:
+        r = fn(*a, **kw)
+        r["wall_s"] = time.perf_counter() - t0
+        return r
+    except Exception as exc:  # noqa: BLE001 -- reported in the JSON line
+        return {"error": f"{type(exc).__name__}: {exc}"[:400], "wall_s": time.perf_counter() - t0}
+    finally:
+        torch.cuda.empty_cache()
 
 
 def main():

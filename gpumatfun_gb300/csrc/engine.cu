@@ -1573,11 +1573,19 @@ int gm_time_loop(gm_handle h, int nsteps, int mode, int use_graph) {
   if (!h) return GM_ERR_ARG;
   if (nsteps < 0 || (mode != 0 && mode != 1)) return fail(h, GM_ERR_ARG, "time_loop: nsteps >= 0 and mode 0 or 1");
   if (h->R != 2) return fail(h, GM_ERR_ARG, "time_loop needs nrhs = 2 (solution and reaction columns)");
+  // Stream capture is not possible on the legacy default stream nor on the
+  // per-thread default stream: refuse before any state changes.
+  if (use_graph && (h->stream == cudaStreamLegacy || h->stream == cudaStreamPerThread))
+    return fail(h, GM_ERR_ARG, "time_loop: a CUDA graph needs a created stream (gm_set_stream with the legacy or "
+                               "per-thread default stream cannot be captured)");
   const int solve = gm::PH_LANCZOS | gm::PH_TRISOLVE | gm::PH_COEF | gm::PH_APPLY | gm::PH_APPLY_SET;
   const int upd = (mode == 0 ? gm::PH_UPDATE_FKPP : gm::PH_UPDATE_FHN) | gm::PH_DEFLATE;
+  // launches inside the loop do not synchronise; the caller's sync mode is
+  // restored on every exit below
   const int saved = h->sync_mode;
   h->sync_mode = 0;
   int rc = GM_OK;
+  cudaError_t st = cudaSuccess;
   if (!use_graph) {
     for (int t = 0; t < nsteps && rc == GM_OK; ++t) {
       rc = launch(h, solve, 4);
@@ -1590,35 +1598,40 @@ int gm_time_loop(gm_handle h, int nsteps, int mode, int use_graph) {
         h->loop_exec = nullptr;
       }
       cudaGraph_t graph = nullptr;
-      GM_CUDA(h, cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-      h->capturing = true;
-      for (int t = 0; t < nsteps && rc == GM_OK; ++t) {
-        rc = launch(h, solve, 4);
-        if (rc == GM_OK) rc = launch(h, upd, 0);
-      }
-      h->capturing = false;
-      cudaError_t st = cudaStreamEndCapture(h->stream, &graph);
-      if (rc == GM_OK && st != cudaSuccess) rc = cuda_fail(h, st, "cudaStreamEndCapture");
+      st = cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal);
+      if (st != cudaSuccess) rc = cuda_fail(h, st, "cudaStreamBeginCapture");
       if (rc == GM_OK) {
-        st = cudaGraphInstantiate(&h->loop_exec, graph, 0);
-        if (st != cudaSuccess) rc = cuda_fail(h, st, "cudaGraphInstantiate");
+        h->capturing = true;
+        for (int t = 0; t < nsteps && rc == GM_OK; ++t) {
+          rc = launch(h, solve, 4);
+          if (rc == GM_OK) rc = launch(h, upd, 0);
+        }
+        h->capturing = false;
+        st = cudaStreamEndCapture(h->stream, &graph);
+        if (rc == GM_OK && st != cudaSuccess) rc = cuda_fail(h, st, "cudaStreamEndCapture");
+        if (rc == GM_OK) {
+          st = cudaGraphInstantiate(&h->loop_exec, graph, 0);
+          if (st != cudaSuccess) rc = cuda_fail(h, st, "cudaGraphInstantiate");
+        }
+        if (graph) cudaGraphDestroy(graph);
       }
-      if (graph) cudaGraphDestroy(graph);
-      if (rc != GM_OK) {
-        h->sync_mode = saved;
-        return rc;
+      if (rc == GM_OK) {
+        h->loop_steps = nsteps;
+        h->loop_mode = mode;
+      } else {
+        h->loop_exec = nullptr;
+        h->loop_steps = h->loop_mode = -1;
       }
-      h->loop_steps = nsteps;
-      h->loop_mode = mode;
     }
-    GM_CUDA(h, cudaEventRecord(h->ev[4][0], h->stream));
-    GM_CUDA(h, cudaGraphLaunch(h->loop_exec, h->stream));
-    GM_CUDA(h, cudaEventRecord(h->ev[4][1], h->stream));
-    h->ev_used[4] = true;
+    if (rc == GM_OK && (st = cudaEventRecord(h->ev[4][0], h->stream)) != cudaSuccess) rc = cuda_fail(h, st, "cudaEventRecord");
+    if (rc == GM_OK && (st = cudaGraphLaunch(h->loop_exec, h->stream)) != cudaSuccess) rc = cuda_fail(h, st, "cudaGraphLaunch");
+    if (rc == GM_OK && (st = cudaEventRecord(h->ev[4][1], h->stream)) != cudaSuccess) rc = cuda_fail(h, st, "cudaEventRecord");
+    if (rc == GM_OK) h->ev_used[4] = true;
   }
   h->sync_mode = saved;
+  if (rc != GM_OK) return rc;
   h->have_V = h->have_y = h->have_coef = true;
-  if (rc == GM_OK && saved) rc = check_sync(h);
+  if (saved) rc = check_sync(h);
   return rc;
 }
 

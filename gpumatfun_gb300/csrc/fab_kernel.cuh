@@ -999,16 +999,38 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
 // off-diagonals beta_r[1..meff-1] and right-hand side -beta0_r w_{r,j} e1.
 // Because the right-hand side is a multiple of e1, the solution needs no
 // back substitution of a general right-hand side: with the bottom-up Schur
-// complements g_q = (alpha_q - s_q) - beta_{q+1}^2 / g_{q+1}, the solution is
-// y_0 = rhs / g_0 and y_q = -beta_q y_{q-1} / g_q.  One warp per system (lane
-// 0; the recurrence is serial), complex FP64, one real division per step; the
-// reciprocals 1/g_q are kept in the tri scratch for the top-down sweep.
+// complements g_q = (alpha_q - s_q) - beta_{q+1} (beta_{q+1} / g_{q+1}), the
+// solution is y_0 = rhs / g_0 and y_q = -beta_q y_{q-1} / g_q.
+// One thread per system (the recurrence is serial in q; neighbouring lanes
+// take neighbouring contour nodes of the same alpha/beta), complex FP64.
+// Scaling: 1/g is Smith's complex reciprocal (R. L. Smith, "Algorithm 116:
+// Complex division", CACM 5(8), 1962), which never forms |g|^2, and the
+// Schur update multiplies beta by (beta / g) instead of forming beta^2, so
+// entries of T up to ~1e300 and down to ~1e-300 neither overflow nor
+// underflow.  The reciprocals 1/g_q are kept in the tri scratch for the
+// top-down sweep.
+
+// 1/(a + ib) by Smith's algorithm: the ratio of the smaller to the larger
+// component keeps every intermediate within the range of the inputs.
+__device__ __forceinline__ void smith_recip(double a, double b, double& rr, double& ri) {
+  if (fabs(a) >= fabs(b)) {
+    const double t = b / a;
+    const double inv = 1.0 / (a + b * t);
+    rr = inv;
+    ri = -t * inv;
+  } else {
+    const double t = a / b;
+    const double inv = 1.0 / (a * t + b);
+    rr = t * inv;
+    ri = -inv;
+  }
+}
+
 template <int R>
 __device__ void phase_trisolve(const KParams& kp, const Ctx& c) {
   const int m = kp.m, C = kp.C;
   const int np = kp.nprob > 0 ? kp.nprob : 1;
-  if (c.lane() != 0) return;
-  for (long long sys = c.gw(); sys < (long long)np * R * C; sys += c.tw()) {
+  for (long long sys = c.gt(); sys < (long long)np * R * C; sys += c.tt()) {
     // sys = (p R + r) C + j for problem p, right-hand side r, node j
     const long long rr = sys / C;
     const int j = (int)(sys % C);
@@ -1024,13 +1046,13 @@ __device__ void phase_trisolve(const KParams& kp, const Ctx& c) {
     const double b0 = be[0];
     const double wr = kp.wts[2LL * C * rr + j], wi = kp.wts[2LL * C * rr + C + j];
     double igr = 0.0, igi = 0.0;   // 1/g_{q+1}
+#pragma unroll 4
     for (int q = me - 1; q >= 0; --q) {
-      const double b2 = q + 1 < me ? be[q + 1] * be[q + 1] : 0.0;
-      const double gr = (al[q] - sh[2 * q]) - b2 * igr;
-      const double gi = -sh[2 * q + 1] - b2 * igi;
-      const double inv = 1.0 / (gr * gr + gi * gi);
-      igr = gr * inv;
-      igi = -gi * inv;
+      const double bq = q + 1 < me ? be[q + 1] : 0.0;
+      // beta^2 / g_{q+1} as beta (beta / g_{q+1})
+      const double gr = (al[q] - sh[2 * q]) - bq * (bq * igr);
+      const double gi = -sh[2 * q + 1] - bq * (bq * igi);
+      smith_recip(gr, gi, igr, igi);
       ig[2 * q] = igr;
       ig[2 * q + 1] = igi;
     }
@@ -1043,6 +1065,7 @@ __device__ void phase_trisolve(const KParams& kp, const Ctx& c) {
       yr[0] = y_r;
       yi[0] = y_i;
     }
+#pragma unroll 4
     for (int q = 1; q < me; ++q) {
       const double tr = -be[q] * y_r, ti = -be[q] * y_i;
       const double gr = ig[2 * q], gi = ig[2 * q + 1];

@@ -22,7 +22,6 @@
 #include <cuda_runtime.h>
 
 #include <cstdio>
-#include <mutex>
 
 #include "../../include/gpumatfun.h"
 #include "fab_kernel.cuh"
@@ -35,10 +34,6 @@ namespace {
 constexpr long long kMaxEntries = GM_NOALLOC_MAX_ENTRIES;
 constexpr long long kScratchDoubles = 4 * kMaxEntries + 4;
 static __device__ __align__(256) double g_noalloc_scratch[kScratchDoubles];
-
-constexpr int kMaxDevices = 64;
-std::mutex g_mu;
-double* g_scratch_ptr[kMaxDevices] = {};
 
 }  // namespace
 
@@ -84,24 +79,15 @@ extern "C" int gm_lin_sys_solves_noalloc(int m, int nrhs, int contour_size, cons
              entries, kMaxEntries);
     return noalloc_fail(GM_ERR_ARG, msg);
   }
-  int dev = 0;
-  cudaError_t st = cudaGetDevice(&dev);
+  cudaError_t st = cudaSuccess;
+  // The host-side name g_noalloc_scratch is only a stand-in: the device
+  // address is looked up on every call, with the caller's device current.
+  // The lookup allocates nothing, and a fresh lookup stays right after a
+  // cudaDeviceReset, which reloads the module at a new address.
+  void* p = nullptr;
+  st = cudaGetSymbolAddress(&p, g_noalloc_scratch);
   if (st != cudaSuccess) return noalloc_fail(GM_ERR_CUDA, cudaGetErrorString(st));
-  if (dev < 0 || dev >= kMaxDevices) return noalloc_fail(GM_ERR_UNSUPPORTED, "lin_sys_solves_noalloc: device id too large");
-  double* scratch = nullptr;
-  {
-    // One-time set-up per device, with that device current: the host-side
-    // name g_noalloc_scratch is only a stand-in, so the device address is
-    // looked up and cached.
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_scratch_ptr[dev]) {
-      void* p = nullptr;
-      st = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      if (st != cudaSuccess) return noalloc_fail(GM_ERR_CUDA, cudaGetErrorString(st));
-      g_scratch_ptr[dev] = static_cast<double*>(p);
-    }
-    scratch = g_scratch_ptr[dev];
-  }
+  double* scratch = static_cast<double*>(p);
   gm::set_global_error("");
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
   gm::KParams kp{};
@@ -116,10 +102,10 @@ extern "C" int gm_lin_sys_solves_noalloc(int m, int nrhs, int contour_size, cons
   int* meff_slots = reinterpret_cast<int*>(scratch + 4 * kMaxEntries);
   k_fill_meff<<<1, 32, 0, s>>>(meff, meff_slots, nrhs, m);
   kp.meff = meff_slots;
-  // one warp per system, as in the engine's lin_sys_solves phase
+  // one thread per system, as in the engine's lin_sys_solves phase
   const int threads = 256;
   const long long systems = (long long)nrhs * contour_size;
-  kp.G = (int)((systems * 32 + threads - 1) / threads);
+  kp.G = (int)((systems + threads - 1) / threads);
   if (nrhs == 1) k_trisolve_noalloc<1><<<kp.G, threads, 0, s>>>(kp);
   if (nrhs == 2) k_trisolve_noalloc<2><<<kp.G, threads, 0, s>>>(kp);
   if (nrhs == 4) k_trisolve_noalloc<4><<<kp.G, threads, 0, s>>>(kp);

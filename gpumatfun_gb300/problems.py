@@ -162,6 +162,28 @@ def disk_mesh(n_target: int, seed: int = 0) -> FEMesh:
     return FEMesh(nodes=pts[perm], tris=inv[tri], boundary=boundary[perm])
 
 
+def submesh(mesh: FEMesh, center=(0.0, 0.0), radius: float = 0.1) -> tuple:
+    """The triangles of ``mesh`` whose three vertices lie within ``radius`` of
+    ``center``, as a mesh of its own: nodes renumbered in their original
+    order, and its boundary the nodes on an edge that only one kept triangle
+    has (plus kept nodes of the original boundary), so that a homogeneous
+    Dirichlet condition there gives an SPD operator.  Returns (submesh,
+    indices of the kept triangles in ``mesh``)."""
+    c = np.asarray(center, dtype=np.float64)
+    inside = np.hypot(mesh.nodes[:, 0] - c[0], mesh.nodes[:, 1] - c[1]) < radius
+    keep = np.flatnonzero(inside[mesh.tris].all(axis=1))
+    tris = mesh.tris[keep]
+    used = np.unique(tris)
+    new_id = np.full(mesh.nodes.shape[0], -1, dtype=np.int64)
+    new_id[used] = np.arange(used.size)
+    t = new_id[tris]
+    edges = np.sort(np.concatenate([t[:, [0, 1]], t[:, [1, 2]], t[:, [2, 0]]]), axis=1)
+    uniq, cnt = np.unique(edges, axis=0, return_counts=True)
+    boundary = mesh.boundary[used].copy()
+    boundary[uniq[cnt == 1].ravel()] = True
+    return FEMesh(nodes=mesh.nodes[used], tris=t, boundary=boundary), keep
+
+
 def gaussian_random_field(points: np.ndarray, sigma: float = 1.0, ell: float = 0.1,
                           seed: int = 0, grid: int = 512) -> np.ndarray:
     """Seeded stationary Gaussian field with squared-exponential covariance

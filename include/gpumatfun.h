@@ -315,7 +315,11 @@ int gm_fe_backward_stored(gm_handle h, const double* g, double* dkappa, double* 
  * (mode 1, FitzHugh-Nagumo).  With use_graph = 1 the nsteps steps are
  * captured once into a CUDA graph (cached per nsteps and mode) and replayed
  * by a single graph launch.  Needs nrhs = 2; the last step's timing is
- * phase slot [4] of gm_phase_times. */
+ * phase slot [4] of gm_phase_times.  use_graph = 1 on the legacy or the
+ * per-thread default stream (which cannot be captured) returns GM_ERR_ARG
+ * before any work.  On every return the handle's synchronous mode is as
+ * before the call, and after a failed call the basis, solves and lift count
+ * as not computed (GM_ERR_STATE from apply_V until the next build). */
 int gm_time_loop(gm_handle h, int nsteps, int mode, int use_graph);
 
 /* Waits for the handle's stream and returns the device status. */
@@ -365,11 +369,13 @@ int gm_get_meff(gm_handle h, int* meff);
  * The only other memory used is a fixed table of 1 MiB + 32 bytes in a
  * file-scope __device__ array, so m * nrhs * C must not exceed
  * GM_NOALLOC_MAX_ENTRIES (GM_ERR_ARG otherwise, message in
- * gm_last_error(NULL)).  The first call on a device looks up the table's
- * device address (once per device, with that device current); make that
- * first call before any stream capture.  All calls share the table and it
- * keeps the last call's contents (no entry needs to start at zero): calls
- * whose kernels overlap on the GPU race and must be ordered on one stream. */
+ * gm_last_error(NULL)).  Every call looks up the table's device address
+ * with the current device (a lookup, no allocation), so the entry point
+ * stays valid across a cudaDeviceReset; the first call on a device also
+ * loads the library's device code there, so make it before any stream
+ * capture.  All calls share the table and it keeps the last call's contents
+ * (no entry needs to start at zero): calls whose kernels overlap on the GPU
+ * race and must be ordered on one stream. */
 int gm_lin_sys_solves_noalloc(int m, int nrhs, int contour_size, const double* aabb, const int* meff,
                               const double* wts, const double* shifts, double* yreal, double* yimag,
                               void* stream);

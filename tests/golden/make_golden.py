@@ -1,7 +1,7 @@
 """Generate the golden fixtures in this directory.
 
-Run in a checkout that has the reference tree available (it reads the FE
-meshes circle1.mat / circle2.mat shipped with GPUMatfun); the outputs are
+Run with GPUMATFUN_REF set to a checkout of the GPUMatfun sources (it reads
+the FE meshes circle1.mat / circle2.mat shipped there); the outputs are
 committed so tests never need the reference at run time.
 
 circle_fab.npz: for each mesh, the operator A = M^{-1/2} K M^{-1/2} restricted
@@ -22,7 +22,7 @@ import scipy.linalg as sla
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
-REF = os.environ.get("GPUMATFUN_REF", "/root/reference")
+REF = os.environ.get("GPUMATFUN_REF")
 
 
 def circle_case(name, seed):
@@ -43,6 +43,8 @@ def circle_case(name, seed):
 
 
 def main():
+    if not REF or not os.path.isdir(REF):
+        raise SystemExit("set GPUMATFUN_REF to a checkout of the GPUMatfun sources (for circle1.mat, circle2.mat)")
     out = {}
     out.update(circle_case("circle1", 11))
     out.update(circle_case("circle2", 12))

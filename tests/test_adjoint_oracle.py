@@ -109,3 +109,21 @@ def test_krylov_gradient_formula_matches_dense(degree, m):
     dk = oadj.krylov_grad(mesh, kappa, o.V, o.Yr, o.Yi, gs, con.weights(f))
     assert np.linalg.norm(o.get_xsol()[:, 1] - db0) <= 1e-7 * np.linalg.norm(db0)
     assert np.linalg.norm(dk - dk0) <= 1e-6 * np.linalg.norm(dk0)
+
+
+def test_submesh_cut_is_a_closed_dirichlet_mesh():
+    """problems.submesh: kept triangles all inside the radius, every edge of
+    the cut that only one kept triangle has is on the Dirichlet boundary, and
+    the restricted operator is SPD."""
+    mesh = problems.disk_mesh(20000, seed=3)
+    sub, keep = problems.submesh(mesh, center=(0.2, -0.1), radius=0.3)
+    cent = np.array([0.2, -0.1])
+    assert np.all(np.hypot(*(mesh.nodes[mesh.tris[keep]] - cent).transpose(2, 0, 1)) < 0.3)
+    np.testing.assert_array_equal(sub.nodes[sub.tris], mesh.nodes[mesh.tris[keep]])
+    e = np.sort(np.concatenate([sub.tris[:, [0, 1]], sub.tris[:, [1, 2]], sub.tris[:, [2, 0]]]), axis=1)
+    uniq, cnt = np.unique(e, axis=0, return_counts=True)
+    assert np.all(sub.boundary[uniq[cnt == 1].ravel()])
+    assert cnt.max() == 2
+    A, *_ = problems.fe_operator(sub, np.ones(sub.tris.shape[0]))
+    assert A.shape[0] == int((~sub.boundary).sum()) > 1000
+    assert np.linalg.eigvalsh(A.toarray()).min() > 0

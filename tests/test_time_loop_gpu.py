@@ -77,3 +77,23 @@ def test_checkpoint_resume_continues_bit_for_bit(engine_lib, monodomain):
     b.time_loop(4, monodomain=monodomain, graph=True)
     np.testing.assert_array_equal(b.get_U(), a.get_U())
     np.testing.assert_array_equal(b.get_state()[1], a.get_state()[1])
+
+
+def test_graph_on_legacy_stream_is_refused_and_handle_stays_synchronous(engine_lib):
+    """A CUDA graph cannot be captured on the legacy default stream: the call
+    is refused up front (GM_ERR_ARG) and the handle keeps its synchronous
+    mode, so the next plain time loop returns with the stream drained and
+    continues the trajectory as a fresh handle would."""
+    import torch
+    from gpumatfun_gb300.engine import GmError
+    P, dt, ode, fhn = workloads.monodomain_problem(64, k=4, m=30, C=16)
+    a = make(P, dt, ode, fhn, sync=True)
+    a.set_stream(0)   # torch's default stream: the legacy default stream
+    with pytest.raises(GmError) as err:
+        a.time_loop(3, monodomain=True, graph=True)
+    assert err.value.code == 1, str(err.value)
+    a.time_loop(20, monodomain=True, graph=False)
+    assert torch.cuda.default_stream().query()   # synchronous mode: nothing left in flight
+    b = make(P, dt, ode, fhn)
+    b.time_loop(20, monodomain=True, graph=False)
+    np.testing.assert_array_equal(a.get_U(), b.get_U())
