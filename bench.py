@@ -67,8 +67,9 @@ def parse():
                     help="L2 bulk prefetch of SELL values: 0 auto (matrix not L2-resident), 1 on, 2 off")
     ap.add_argument("--reorth", type=int, default=0, choices=[0, 1, 2],
                     help="Gram-Schmidt reorthogonalisation passes per Lanczos step (0: the reference's recurrence)")
-    ap.add_argument("--l2-window", type=int, default=0, choices=[0, 1],
-                    help="0: keep the SELL matrix in L2 (persisting window), 1: off")
+    ap.add_argument("--l2-window", type=int, default=0, choices=[0, 1, 2],
+                    help="0: keep the SELL matrix in L2 (persisting window) when it and one pass's vectors "
+                         "fit, 1: off, 2: on whenever the matrix fits the persisting limit")
     return ap.parse_args()
 
 
@@ -242,7 +243,8 @@ def config_of(args, P):
             "d": int(P.d), "k": int(P.k), "nrhs": int(args.nrhs), "precision": args.precision,
             "f": P.meta.get("f", "x^-0.8" if "disk" in P.name else "exp(-tau x^(alpha/2))"),
             "l2": "inputs larger than L2 (Krylov basis m x n x 8 B per RHS)",
-            "l2_window": "SELL matrix persisting in L2" if args.l2_window == 0 else "off",
+            "l2_window": ["auto (SELL matrix persisting in L2 when it and one pass's vectors fit)", "off",
+                          "on"][args.l2_window],
             "reorth": ["none (reference recurrence)", "CGS", "CGS2"][args.reorth],
             "parallelism": f"replicas x{args.gpus}"}
 

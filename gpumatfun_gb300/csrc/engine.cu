@@ -576,6 +576,39 @@ cudaError_t raise_smem_limit(int dev, void* kfn, size_t bytes) {
   return st;
 }
 
+// The persisting L2 set-aside (cudaLimitPersistingL2CacheSize) belongs to
+// the context, not to a handle: left set after its handle is gone, it keeps
+// a share of L2 out of reach of ordinary accesses of every later kernel
+// (measured: a 3D 256^3 FP64 solve created after a deleted handle with a
+// window ran 13% slower).  Handles with a window count themselves per
+// device; the set-aside is raised to the largest live window and returned
+// to zero with the last one.
+std::mutex g_window_mu;
+std::map<int, std::pair<int, size_t>> g_window_users;   // device -> (handles, set-aside bytes)
+
+cudaError_t window_acquire(int dev, size_t bytes) {
+  std::lock_guard<std::mutex> lock(g_window_mu);
+  auto& u = g_window_users[dev];
+  if (bytes > u.second) {
+    const cudaError_t st = cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, bytes);
+    if (st != cudaSuccess) return st;
+    u.second = bytes;
+  }
+  u.first++;
+  return cudaSuccess;
+}
+
+void window_release(int dev) {
+  std::lock_guard<std::mutex> lock(g_window_mu);
+  auto it = g_window_users.find(dev);
+  if (it == g_window_users.end() || it->second.first <= 0) return;
+  if (--it->second.first == 0) {
+    cudaCtxResetPersistingL2Cache();
+    cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, 0);
+    it->second.second = 0;
+  }
+}
+
 void* pick_kernel(int prec, int R, int group) {
   return prec == GM_FP64 ? gm::kernel_fp64(R, group) : gm::kernel_mixed(R, group);
 }
@@ -704,7 +737,13 @@ int set_usol(gm_engine* e, const double* U, bool on_device, bool scaled = true) 
 void destroy(gm_engine* e) {
   if (!e) return;
   if (e->stream) cudaStreamSynchronize(e->stream);
-  if (e->l2_window) cudaCtxResetPersistingL2Cache();
+  if (e->l2_window) {
+    int cur = 0;
+    cudaGetDevice(&cur);
+    cudaSetDevice(e->dev);
+    window_release(e->dev);
+    cudaSetDevice(cur);
+  }
   if (e->loop_exec) cudaGraphExecDestroy(e->loop_exec);
   for (auto& b : e->bufs) cudaFree(b.p);
   e->bufs.clear();
@@ -820,16 +859,31 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
   // persisting window (see below) gains nothing, so by default the prefetch
   // is on only when the matrix does not fit that window.
   if (a->val_prefetch < 0 || a->val_prefetch > 2) return fail(e, GM_ERR_ARG, "val_prefetch must be 0, 1 or 2");
+  if (a->l2_window < 0 || a->l2_window > 2) return fail(e, GM_ERR_ARG, "l2_window must be 0 (auto), 1 (off) or 2 (on)");
+  // The persisting L2 window pays when the whole matrix fits the persisting
+  // limit and the rest of L2 still holds one SpMV pass's vectors: the
+  // gathered input and the output (n R Horner elements each, 8 bytes: FP64
+  // or float-float) and the basis row read (n R storage elements).  When
+  // they do not fit, a pinned matrix makes the vectors, whose gathers are
+  // latency-critical, stream from DRAM on every pass; streaming the matrix
+  // with the value prefetch instead keeps the vectors in L2 (measured on the
+  // 1M-node FE disk with 4 right-hand sides, mixed precision: with the
+  // window the launch moved its whole algorithmic traffic through DRAM at
+  // an L2 hit rate of 13%).
+  bool use_window = false;
+  if (a->l2_window != 1 && e->mat_bytes > 0) {
+    int mp = 0, mw = 0, l2 = 0;
+    GM_CUDA(e, cudaDeviceGetAttribute(&mp, cudaDevAttrMaxPersistingL2CacheSize, e->dev));
+    GM_CUDA(e, cudaDeviceGetAttribute(&mw, cudaDevAttrMaxAccessPolicyWindowSize, e->dev));
+    GM_CUDA(e, cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, e->dev));
+    const bool fits_limit = mp > 0 && mw > 0 && e->mat_bytes <= (size_t)std::min(mp, mw);
+    const double vec_bytes = (double)ntot * e->R * (2.0 * 8.0 + (e->prec == GM_FP64 ? 8.0 : 4.0));
+    const bool fits_l2 = (double)e->mat_bytes + vec_bytes <= 0.9 * (double)l2;
+    use_window = fits_limit && (a->l2_window == 2 || fits_l2);
+  }
   e->kp.pf_vals = 0;
   if (stage_cap > 0 && a->val_prefetch != 2) {
-    bool l2_resident = false;
-    if (a->l2_window == 0 && e->mat_bytes > 0) {
-      int mp = 0, mw = 0;
-      GM_CUDA(e, cudaDeviceGetAttribute(&mp, cudaDevAttrMaxPersistingL2CacheSize, e->dev));
-      GM_CUDA(e, cudaDeviceGetAttribute(&mw, cudaDevAttrMaxAccessPolicyWindowSize, e->dev));
-      l2_resident = mp > 0 && mw > 0 && e->mat_bytes <= (size_t)std::min(mp, mw);
-    }
-    if (a->val_prefetch == 1 || !l2_resident) e->kp.pf_vals = e->prec == GM_FP64 ? 8 : 4;
+    if (a->val_prefetch == 1 || !use_window) e->kp.pf_vals = e->prec == GM_FP64 ? 8 : 4;
   }
   // Grid: blocks_per_sm x SMs, capped by co-residency of each phase-group
   // kernel and by the work (about one SELL slice per warp: small problems
@@ -885,26 +939,23 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
     }
   }
   csr = Csr();
-  if (a->l2_window == 0 && e->mat_bytes > 0) {
-    // Persisting L2 lines for the matrix, which every SpMV pass re-reads: the
-    // set-aside is this context's (released with it); the hit ratio spreads
-    // the limit over the window when the matrix is larger than the limit.
-    int max_persist = 0, max_window = 0;
-    GM_CUDA(e, cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, e->dev));
+  if (use_window) {
+    // Persisting L2 lines for the matrix, which every SpMV pass re-reads
+    // (only when the whole matrix fits the persisting limit: a partial
+    // window pins a sliver of a large matrix and takes L2 from the vectors).
+    // The set-aside is a setting of the context, shared by all handles: it
+    // is raised to the largest live window and released when the last
+    // handle with a window is deleted (window_acquire / window_release).
+    int max_window = 0;
     GM_CUDA(e, cudaDeviceGetAttribute(&max_window, cudaDevAttrMaxAccessPolicyWindowSize, e->dev));
-    // only when the whole matrix fits the persisting set-aside: a partial
-    // window pins a sliver of a large matrix and takes L2 from the vectors
-    if (max_persist > 0 && max_window > 0 && e->mat_bytes <= (size_t)std::min(max_persist, max_window)) {
-      const size_t win = std::min<size_t>(e->mat_bytes, (size_t)max_window);
-      const size_t setaside = std::min<size_t>(win, (size_t)max_persist);
-      GM_CUDA(e, cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, setaside));
-      e->window.base_ptr = e->mat_base;
-      e->window.num_bytes = win;
-      e->window.hitRatio = (float)std::min(1.0, (double)setaside / (double)win);
-      e->window.hitProp = cudaAccessPropertyPersisting;
-      e->window.missProp = cudaAccessPropertyStreaming;
-      e->l2_window = true;
-    }
+    const size_t win = std::min<size_t>(e->mat_bytes, (size_t)max_window);
+    GM_CUDA(e, window_acquire(e->dev, win));
+    e->window.base_ptr = e->mat_base;
+    e->window.num_bytes = win;
+    e->window.hitRatio = 1.0f;
+    e->window.hitProp = cudaAccessPropertyPersisting;
+    e->window.missProp = cudaAccessPropertyStreaming;
+    e->l2_window = true;
   }
 
   KParams& kp = e->kp;

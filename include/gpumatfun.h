@@ -114,7 +114,10 @@ typedef struct gm_create_args {
                                   to device slots, needed by gm_fe_attach          */
   int l2_window;               /* 0 = launches keep the SELL matrix resident in L2
                                   (persisting access-policy window) when it fits
-                                  the device's persisting limit (default), 1 = off */
+                                  the device's persisting limit and the matrix plus
+                                  one SpMV pass's vectors fit in L2 (default),
+                                  1 = off, 2 = on whenever the matrix fits the
+                                  persisting limit                                 */
   const double* row_weight;    /* mixed engine, n entries: the FP32-stored matrix
                                   gets a per-row diagonal correction so that
                                   A' w = A w exactly for this w (the operator's
