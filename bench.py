@@ -409,6 +409,7 @@ def run_ours(args, P, rank, world, local):
                 "note": "mixed engine, 4 right-hand sides per launch, over the plain FP64 engine with one "
                         "right-hand side per launch; fused launches on both sides"}
         line["adjoint_250k"] = _extra("adjoint_250k", adjoint_measure, 250_000, 3, 2)
+        line["deflation_gpu"] = _extra("deflation_gpu", deflation_measure, P)
     if rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(P, host_deflate(P, P.U), args.cpu_sample_s, 0)
     if rank == 0:
@@ -830,6 +831,26 @@ def fd3d_measure(N: int, K: int, W: int) -> dict:
     out["mixed_over_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
     out["setup_s"] = setup_s
     return out
+
+
+def deflation_measure(P) -> dict:
+    """The workload's k deflation pairs computed on the GPU
+    (gm_deflation_pairs: Chebyshev-filtered subspace iteration, FP64) against
+    the host shift-invert eigsh pairs the workload was built with: time,
+    eigenvalue agreement, residuals and the angle between the subspaces."""
+    from gpumatfun_gb300 import eigs
+    t0 = time.perf_counter()
+    lam, Q, st = eigs.deflation_pairs(P.A, P.k)
+    wall = time.perf_counter() - t0
+    res = np.linalg.norm(P.A @ Q - Q * lam, axis=0) / np.abs(lam)
+    cos = np.linalg.svd(P.Q.T @ Q, compute_uv=False)
+    return {"k": int(P.k), "device_s": st["device_s"], "call_wall_s": wall, "iterations": st["iterations"],
+            "block_spmvs": st["block_spmvs"], "block_width": 32,
+            "max_rel_residual": float(res.max()), "eig_rel_err_vs_eigsh": float(np.max(np.abs(lam - P.lam) / P.lam)),
+            "subspace_cos_min_vs_eigsh": float(cos.min()),
+            "host_eigsh_s": P.meta.get("eigsh_s"),
+            "note": "host_eigsh_s: scipy shift-invert eigsh (k + 1 pairs, sparse LU) when the workload was built "
+                    "on this host"}
 
 
 def _extra(name, fn, *a, **kw):

@@ -16,7 +16,7 @@ CSRC = PKG / "csrc"
 LIBDIR = PKG / "_lib"
 LIB = Path(os.environ["GPUMATFUN_LIB"]) if os.environ.get("GPUMATFUN_LIB") else LIBDIR / "libgpumatfun.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["engine.cu", "kern_fp64.cu", "kern_mixed.cu", "noalloc.cu"]
+SOURCES = ["engine.cu", "kern_fp64.cu", "kern_mixed.cu", "noalloc.cu", "eigs.cu"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC"]
 # Kernel shape overrides for tuning builds, e.g. "-DGM_MINB=1 -DGM_CH1=8"
 # (GM_MINB: minimum resident 512-thread blocks per SM; GM_CH1/2/4: SpMV chunk

@@ -24,7 +24,8 @@ __all__ = ["GmError", "Engine", "LanczosEngine", "load_library", "EXPORTED_SYMBO
 GM_FP64, GM_MIXED = 0, 1
 GM_CSC, GM_CSR = 0, 1
 _STATUS = {0: "GM_OK", 1: "GM_ERR_ARG", 2: "GM_ERR_OOM", 3: "GM_ERR_CUDA", 4: "GM_ERR_BREAKDOWN",
-           5: "GM_ERR_TIMEOUT", 6: "GM_ERR_STATE", 7: "GM_ERR_NONFINITE", 8: "GM_ERR_UNSUPPORTED"}
+           5: "GM_ERR_TIMEOUT", 6: "GM_ERR_STATE", 7: "GM_ERR_NONFINITE", 8: "GM_ERR_UNSUPPORTED",
+           9: "GM_ERR_NOCONV"}
 
 EXPORTED_SYMBOLS = [
     "gm_default_args", "gm_lanczos_create", "gm_lanczos_delete", "gm_build_subspace",
@@ -34,7 +35,7 @@ EXPORTED_SYMBOLS = [
     "gm_phase_times", "gm_info", "gm_get_meff", "gm_last_error", "gm_version",
     "gm_lin_sys_solves_noalloc", "gm_batch_create", "gm_time_loop", "gm_fe_attach", "gm_fe_assemble",
     "gm_fe_gradient", "gm_get_solution_device", "gm_fe_forward", "gm_fe_backward",
-    "gm_fe_backward_stored", "gm_get_basis", "gm_get_ode", "gm_set_state",
+    "gm_fe_backward_stored", "gm_get_basis", "gm_get_ode", "gm_set_state", "gm_deflation_pairs",
 ]
 
 _dp = ct.POINTER(ct.c_double)
@@ -120,6 +121,8 @@ def load_library(build_if_missing: bool = False) -> ct.CDLL:
     lib.gm_phase_times.argtypes = [h, ct.POINTER(ct.c_float)]
     lib.gm_info.argtypes = [h, _lp]
     lib.gm_get_meff.argtypes = [h, ct.POINTER(ct.c_int)]
+    lib.gm_deflation_pairs.argtypes = [ct.c_int64, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_double,
+                                       ct.c_int, ct.c_int, ct.c_uint64, ct.c_void_p, ct.c_void_p, _dp]
     lib.gm_last_error.argtypes = [h]
     lib.gm_last_error.restype = ct.c_char_p
     lib.gm_version.restype = ct.c_char_p

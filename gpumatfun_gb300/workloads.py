@@ -167,9 +167,12 @@ def fe_disk_problem(n_target: int, k: int, m: int, C: int, degree: int, alpha: f
     kappa = np.exp(g)
     A, ms, inner = problems.fe_operator(mesh, kappa)
     n = A.shape[0]
+    import time
     import scipy.sparse.linalg as sla
     lmax = float(sla.eigsh(A, k=1, which="LA", return_eigenvectors=False, tol=1e-6)[0]) * 1.01
+    timing = {}
     if k > 0:
+        t0 = time.perf_counter()
         if deflation == "eigsh":
             # shift-invert at 0 with a symmetric minimum-degree ordering of the LU
             # (about 2x cheaper than scipy's default COLAMD on 2D meshes)
@@ -177,8 +180,13 @@ def fe_disk_problem(n_target: int, k: int, m: int, C: int, degree: int, alpha: f
             op = sla.LinearOperator(A.shape, matvec=lu.solve, dtype=np.float64)
             lam, Q = sla.eigsh(A, k=k + 1, sigma=0.0, which="LM", OPinv=op, tol=1e-10)
             del lu
+        elif deflation == "gpu":
+            # Chebyshev-filtered subspace iteration on the GPU (gm_deflation_pairs)
+            from . import eigs
+            lam, Q, _ = eigs.deflation_pairs(A, k + 1)
         else:
             raise ValueError(deflation)
+        timing[f"{deflation}_s"] = time.perf_counter() - t0
         o = np.argsort(lam)
         lam, Q = lam[o], Q[:, o]
         l1 = float(lam[k])  # first eigenvalue left after deflating k
@@ -192,7 +200,8 @@ def fe_disk_problem(n_target: int, k: int, m: int, C: int, degree: int, alpha: f
     U /= np.linalg.norm(U, axis=0, keepdims=True)
     f = params.frac_power(-alpha / 2)
     return make_problem(name, A, U, Q, lam, [f] * R, m, C, l1, lmax, degree=degree,
-                        prob_dim=lmax / 4, meta=dict(n_target=n_target, nt=mesh.tris.shape[0], seed=seed),
+                        prob_dim=lmax / 4, meta=dict(n_target=n_target, nt=mesh.tris.shape[0], seed=seed,
+                                                     deflation=deflation, **timing),
                         row_weight=ms)
 
 
@@ -233,13 +242,16 @@ def cached_problem(name: str, R: int = 1, cache_dir: str | None = None, seed: in
             rng = np.random.default_rng(seed + 2)
             U = rng.random((A.shape[0], R))
             U /= np.linalg.norm(U, axis=0, keepdims=True)
+        meta = dict(n_target=n_target, seed=seed, cached=True)
+        if "eigsh_s" in z:
+            meta["eigsh_s"] = float(z["eigsh_s"])
         return make_problem(f"fe-disk-{tag}-fp64", A, U[:, :R], z["Q"], z["lam"], [f] * R, 80, 48,
                             float(z["l1"]), float(z["lN"]), degree=8, prob_dim=float(z["lN"]) / 4,
-                            meta=dict(n_target=n_target, seed=seed, cached=True), row_weight=z["ms"])
+                            meta=meta, row_weight=z["ms"])
     P = fe_disk_problem(n_target, 20, 80, 48, 8, alpha=alpha, R=max(R, 4), seed=seed, name=f"fe-disk-{tag}-fp64")
     tmp = path + f".tmp{os.getpid()}.npz"
     np.savez(tmp, data=P.A.data, indices=P.A.indices, indptr=P.A.indptr, shape=np.array(P.A.shape),
-             U=P.U, Q=P.Q, lam=P.lam, l1=P.l1, lN=P.lN, ms=P.row_weight)
+             U=P.U, Q=P.Q, lam=P.lam, l1=P.l1, lN=P.lN, ms=P.row_weight, eigsh_s=P.meta.get("eigsh_s", np.nan))
     os.replace(tmp, path)
     return make_problem(P.name, P.A, P.U[:, :R], P.Q, P.lam, [f] * R, 80, 48, P.l1, P.lN, degree=8,
                         prob_dim=P.lN / 4, meta=P.meta, row_weight=P.row_weight)

@@ -42,7 +42,8 @@ typedef enum gm_status {
   GM_ERR_TIMEOUT = 5,      /* a bounded grid-barrier wait expired               */
   GM_ERR_STATE = 6,        /* call out of order (e.g. apply before solves)      */
   GM_ERR_NONFINITE = 7,    /* NaN/Inf met in the recurrence                     */
-  GM_ERR_UNSUPPORTED = 8   /* option not available on this device/build         */
+  GM_ERR_UNSUPPORTED = 8,  /* option not available on this device/build         */
+  GM_ERR_NOCONV = 9        /* iteration limit reached before the tolerance      */
 } gm_status;
 
 typedef enum gm_precision {
@@ -382,6 +383,31 @@ int gm_get_meff(gm_handle h, int* meff);
 int gm_lin_sys_solves_noalloc(int m, int nrhs, int contour_size, const double* aabb, const int* meff,
                               const double* wts, const double* shifts, double* yreal, double* yimag,
                               void* stream);
+
+/* The k smallest eigenpairs of the symmetric matrix A (n x n, CSR: int64
+ * row pointer, int32 column indices, FP64 values; host or device memory),
+ * for the engine's deflation vectors Q and lambda.  Replaces the host
+ * eigensolve of the reference's set-up, eigs(K, M, k, 'sm') on the
+ * generalised problem (process_nonuniform.m:38-40, 106-110; with the lumped
+ * mass M this is the symmetric A = M^{-1/2} K M^{-1/2} the engine takes).
+ *
+ * Method: Chebyshev-filtered subspace iteration over a block of 32 vectors on
+ * the GPU, all in FP64: scaled Chebyshev filter on [largest Ritz value,
+ * Gershgorin bound], CholQR2, Rayleigh-Ritz with a Jacobi eigensolver of the
+ * 32 x 32 projection.  1 <= k <= 24, n >= 64.  Iterates until every wanted
+ * relative residual ||A q_j - lambda_j q_j|| / |lambda_j| <= tol, or for at
+ * most max_iter filter applications of degree <= max_degree; seed fixes the
+ * start block.  Outputs (host or device): lambda (k, ascending) and Q (n x k,
+ * column-major, orthonormal columns).  stats (8 doubles, may be NULL):
+ * [0] iterations, [1] block SpMVs, [2] device seconds, [3] largest wanted
+ * relative residual, [4] Gershgorin bound, [5] last filter cut, [6] largest
+ * Ritz value of the block, [7] nnz.  Returns GM_ERR_NOCONV (outputs and stats
+ * still written) when the tolerance was not reached; messages in
+ * gm_last_error(NULL).  Allocates about 6 n 256 + 12 nnz bytes of device
+ * memory for the duration of the call and synchronises the device. */
+int gm_deflation_pairs(int64_t n, const int64_t* rowptr, const int32_t* col, const double* val, int k,
+                       double tol, int max_degree, int max_iter, uint64_t seed, double* lambda, double* Q,
+                       double* stats);
 
 /* Last error message of h (or of the last failed create when h is NULL). */
 const char* gm_last_error(gm_handle h);

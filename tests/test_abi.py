@@ -64,3 +64,19 @@ def test_create_rejects_bad_arguments_before_device(engine_lib):
         assert msg in engine_lib.gm_last_error(None).decode(), engine_lib.gm_last_error(None)
         assert not h.value
     assert engine_lib.gm_lanczos_create(None, ct.byref(h)) == 1
+
+
+def test_deflation_pairs_argument_checks(engine_lib):
+    """gm_deflation_pairs rejects bad sizes before any device work."""
+    rp = np.zeros(2, dtype=np.int64)
+    ci = np.zeros(1, dtype=np.int32)
+    va = np.zeros(1)
+    out = np.zeros(4)
+    f = engine_lib.gm_deflation_pairs
+    f.argtypes = [ct.c_int64, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_double, ct.c_int, ct.c_int,
+                  ct.c_uint64, ct.c_void_p, ct.c_void_p, ct.c_void_p]
+    for n, k, tol in ((10, 2, 1e-8), (1000, 0, 1e-8), (1000, 25, 1e-8), (1000, 4, 0.0)):
+        rc = f(n, rp.ctypes.data, ci.ctypes.data, va.ctypes.data, k, tol, 100, 10, 0, out.ctypes.data,
+               out.ctypes.data, None)
+        assert rc == 1, (n, k, tol)
+        assert b"deflation_pairs" in engine_lib.gm_last_error(None)
