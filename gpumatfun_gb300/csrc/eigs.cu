@@ -38,6 +38,7 @@
 #include <vector>
 
 #include "../../include/gpumatfun.h"
+#include "fab_common.cuh"
 
 namespace gm {
 void set_global_error(const char* msg);  // engine.cu: the text gm_last_error(NULL) returns
@@ -47,6 +48,7 @@ namespace {
 
 constexpr int P = 32;            // block width: one column per lane
 constexpr double kCondCap = 1e4;  // largest amplification of a0 over a per filter
+constexpr double kFFUntil = 1e-7; // float-float filter while the wanted residuals are above this
 
 int eig_fail(int code, const char* fmt, ...) {
   char buf[512];
@@ -58,39 +60,110 @@ int eig_fail(int code, const char* fmt, ...) {
   return code;
 }
 
-// Y_out = c1 (A X) + c2 X + c3 Y_prev, one warp per row, lane = column.
-// Stored entries of a row are taken 8 at a time: their column indices and
-// values are read with warp-uniform loads, then the 8 gathered rows of X are
-// all in flight before the products.
+// Y_out = c1 (A X) + c2 X + c3 Y_prev, lane = column, one warp per row.
+// A row has few stored entries, so the kernel waits on the dependent chain
+// of memory accesses (row pointer, then column indices and values, then the
+// gathered rows of X).  The chain is shortened: the next row's pointers are
+// loaded while the current row is processed, and the epilogue's X and Y_prev
+// rows are loaded before the gathers.  Entries are taken 8 at a time, their
+// gathers all in flight before the products.
 __global__ void k_cheb(long long n, const long long* __restrict__ rp, const int* __restrict__ ci,
                        const double* __restrict__ va, const double* __restrict__ X,
                        const double* __restrict__ Yp, double* __restrict__ Yo, double c1, double c2, double c3) {
   const int lane = threadIdx.x & 31;
   const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
-  for (long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; r < n; r += nw) {
-    const long long b = rp[r], e = rp[r + 1];
+  long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  long long b = r < n ? rp[r] : 0, e = r < n ? rp[r + 1] : 0;
+  for (; r < n; r += nw) {
+    const long long rn = r + nw;
+    const long long bn = rn < n ? rp[rn] : 0, en = rn < n ? rp[rn + 1] : 0;
+    const double xo = c2 != 0.0 ? X[r * P + lane] : 0.0;
+    const double yo = c3 != 0.0 ? Yp[r * P + lane] : 0.0;
     double acc = 0.0;
     for (long long t = b; t < e; t += 8) {
       double av[8], xv[8];
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
+        av[q] = 0.0;
+        xv[q] = 0.0;
         if (t + q < e) {
-          const int c = __ldg(ci + t + q);
           av[q] = __ldg(va + t + q);
-          xv[q] = __ldg(X + (long long)c * P + lane);
-        } else {
-          av[q] = 0.0;
-          xv[q] = 0.0;
+          xv[q] = __ldg(X + (long long)__ldg(ci + t + q) * P + lane);
         }
       }
 #pragma unroll
       for (int q = 0; q < 8; ++q) acc = fma(av[q], xv[q], acc);
     }
-    double y = c1 * acc;
-    if (c2 != 0.0) y = fma(c2, X[r * P + lane], y);
-    if (c3 != 0.0) y = fma(c3, Yp[r * P + lane], y);
-    Yo[r * P + lane] = y;
+    Yo[r * P + lane] = fma(c3, yo, fma(c2, xo, c1 * acc));
+    b = bn;
+    e = en;
   }
+}
+
+// The same three-term step in float-float arithmetic on the FP32 pipe
+// (about 48 significant bits): values split as hi + lo floats, block vectors
+// as (hi, lo) pairs.  Each product is hi*hi exactly (two_prod) plus the two
+// cross terms; the row sum keeps its hi part by two_sum and collects every
+// rounding error in lo, renormalised once per row.  About 12 FP32
+// instructions per product instead of one FP64 FMA on GB300's narrow FP64
+// pipe.  Memory access order as in k_cheb.
+__global__ void k_cheb_ff(long long n, const long long* __restrict__ rp, const int* __restrict__ ci,
+                          const float* __restrict__ vhi, const float* __restrict__ vlo,
+                          const float2* __restrict__ X, const float2* __restrict__ Yp, float2* __restrict__ Yo,
+                          float2 c1, float2 c2, float2 c3) {
+  using gm::ff;
+  const int lane = threadIdx.x & 31;
+  const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+  const float2 z = make_float2(0.f, 0.f);
+  long long r = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  long long b = r < n ? rp[r] : 0, e = r < n ? rp[r + 1] : 0;
+  for (; r < n; r += nw) {
+    const long long rn = r + nw;
+    const long long bn = rn < n ? rp[rn] : 0, en = rn < n ? rp[rn + 1] : 0;
+    const float2 xo = c2.x != 0.f ? X[r * P + lane] : z;
+    const float2 yo = c3.x != 0.f ? Yp[r * P + lane] : z;
+    float ahi = 0.f, alo = 0.f;
+    for (long long t = b; t < e; t += 8) {
+      float2 av[8], xv[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        av[q] = z;
+        xv[q] = z;
+        if (t + q < e) {
+          av[q] = make_float2(__ldg(vhi + t + q), __ldg(vlo + t + q));
+          xv[q] = __ldg(X + (long long)__ldg(ci + t + q) * P + lane);
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const ff p = gm::two_prod(av[q].x, xv[q].x);
+        const float cross = fmaf(av[q].x, xv[q].y, av[q].y * xv[q].x);
+        const ff s2 = gm::two_sum(ahi, p.hi);
+        ahi = s2.hi;
+        alo += s2.lo + (p.lo + cross);
+      }
+    }
+    ff y = gm::ff_mul(gm::fast_two_sum(ahi, alo), ff{c1.x, c1.y});
+    if (c2.x != 0.f) y = gm::ff_add(y, gm::ff_mul(ff{xo.x, xo.y}, ff{c2.x, c2.y}));
+    if (c3.x != 0.f) y = gm::ff_add(y, gm::ff_mul(ff{yo.x, yo.y}, ff{c3.x, c3.y}));
+    Yo[r * P + lane] = make_float2(y.hi, y.lo);
+    b = bn;
+    e = en;
+  }
+}
+
+// FP64 block <-> float-float block (hi = fl32(x), lo = fl32(x - hi))
+__global__ void k_d2ff(long long count, const double* __restrict__ x, float2* __restrict__ y) {
+  const long long nt = (long long)gridDim.x * blockDim.x;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += nt) {
+    const float h = (float)x[t];
+    y[t] = make_float2(h, (float)(x[t] - (double)h));
+  }
+}
+__global__ void k_ff2d(long long count, const float2* __restrict__ x, double* __restrict__ y) {
+  const long long nt = (long long)gridDim.x * blockDim.x;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < count; t += nt)
+    y[t] = (double)x[t].x + (double)x[t].y;
 }
 
 // partial[blk][i * 32 + j] = sum over the block's rows of Y[r][i] Z[r][j]
@@ -293,17 +366,22 @@ struct Solver {
   long long* rp = nullptr;
   int* ci = nullptr;
   double* va = nullptr;
+  float* vhi = nullptr;     // float-float split of the values (float-float filter)
+  float* vlo = nullptr;
+  unsigned grid64 = 0, grid_ff = 0;   // resident 256-thread blocks of k_cheb / k_cheb_ff
   double* buf[6] = {};      // block vectors [n][32]
   double* part = nullptr;   // Gram partials [G][1024]
   double* small = nullptr;  // [0] G/H 1024, [1024] M/W 1024, [2048] theta 32
   int* status = nullptr;
-  long long spmm = 0;
+  long long spmm = 0, spmm_ff = 0;
   std::string err;
 
   ~Solver() {
     cudaFree(rp);
     cudaFree(ci);
     cudaFree(va);
+    cudaFree(vhi);
+    cudaFree(vlo);
     for (double* b : buf) cudaFree(b);
     cudaFree(part);
     cudaFree(small);
@@ -313,8 +391,20 @@ struct Solver {
   unsigned grid_rows() const { return (unsigned)std::max(1, nsm * 8); }   // 256-thread blocks, a warp per row
 
   cudaError_t spmm_axpby(const double* X, const double* Yp, double* Yo, double c1, double c2, double c3) {
-    k_cheb<<<grid_rows(), 256>>>(n, rp, ci, va, X, Yp, Yo, c1, c2, c3);
+    k_cheb<<<grid64, 256>>>(n, rp, ci, va, X, Yp, Yo, c1, c2, c3);
     ++spmm;
+    return cudaGetLastError();
+  }
+
+  static float2 to_ff(double v) {
+    const float h = (float)v;
+    return make_float2(h, (float)(v - (double)h));
+  }
+
+  cudaError_t spmm_axpby_ff(const float2* X, const float2* Yp, float2* Yo, double c1, double c2, double c3) {
+    k_cheb_ff<<<grid_ff, 256>>>(n, rp, ci, vhi, vlo, X, Yp, Yo, to_ff(c1), to_ff(c2), to_ff(c3));
+    ++spmm;
+    ++spmm_ff;
     return cudaGetLastError();
   }
 
@@ -346,6 +436,9 @@ struct Solver {
 extern "C" int gm_deflation_pairs(int64_t n, const int64_t* rowptr, const int32_t* col, const double* val, int k,
                                   double tol, int max_degree, int max_iter, uint64_t seed, double* lambda, double* Q,
                                   double* stats) {
+  // a negative max_degree selects the FP64 filter throughout (|max_degree| is the cap)
+  const bool use_ff_arg = max_degree >= 0;
+  max_degree = max_degree < 0 ? -max_degree : max_degree;
   gm::set_global_error("");
   if (n < 2 * P) return eig_fail(GM_ERR_ARG, "deflation_pairs: n must be at least %d", 2 * P);
   if (k < 1 || k > P - 8) return eig_fail(GM_ERR_ARG, "deflation_pairs: k must be in [1, %d]", P - 8);
@@ -366,13 +459,14 @@ extern "C" int gm_deflation_pairs(int64_t n, const int64_t* rowptr, const int32_
   if ((st = cudaMemcpy(hci.data(), col, sizeof(int32_t) * nnz, cudaMemcpyDefault)) != cudaSuccess ||
       (st = cudaMemcpy(hva.data(), val, sizeof(double) * nnz, cudaMemcpyDefault)) != cudaSuccess)
     return eig_fail(GM_ERR_CUDA, "deflation_pairs: matrix copy: %s", cudaGetErrorString(st));
-  double b = 0.0;
+  double b = 0.0, vmin = HUGE_VAL;
   for (long long i = 0; i < n; ++i) {
     double s = 0.0;
     for (long long t = hrp[i]; t < hrp[i + 1]; ++t) {
       if (hci[t] < 0 || hci[t] >= n) return eig_fail(GM_ERR_ARG, "deflation_pairs: column index out of range");
       if (!std::isfinite(hva[t])) return eig_fail(GM_ERR_ARG, "deflation_pairs: non-finite matrix value");
       s += std::fabs(hva[t]);
+      if (hva[t] != 0.0) vmin = std::min(vmin, std::fabs(hva[t]));
     }
     b = std::max(b, s);
   }
@@ -400,6 +494,29 @@ extern "C" int gm_deflation_pairs(int64_t n, const int64_t* rowptr, const int32_
     cudaGetLastError();
     return eig_fail(GM_ERR_OOM, "deflation_pairs: device allocation of %.1f GB failed", (6.0 * vbytes + 12.0 * nnz) / 1e9);
   }
+  {
+    std::vector<float> hi(nnz), lo(nnz);
+    for (long long t = 0; t < nnz; ++t) {
+      hi[t] = (float)hva[t];
+      lo[t] = (float)(hva[t] - (double)hi[t]);
+    }
+    if (alloc((void**)&S.vhi, sizeof(float) * nnz) != cudaSuccess || alloc((void**)&S.vlo, sizeof(float) * nnz) != cudaSuccess) {
+      cudaGetLastError();
+      return eig_fail(GM_ERR_OOM, "deflation_pairs: device allocation failed");
+    }
+    if ((st = cudaMemcpy(S.vhi, hi.data(), sizeof(float) * nnz, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (st = cudaMemcpy(S.vlo, lo.data(), sizeof(float) * nnz, cudaMemcpyHostToDevice)) != cudaSuccess)
+      return eig_fail(GM_ERR_CUDA, "deflation_pairs: upload: %s", cudaGetErrorString(st));
+  }
+  {
+    // grids of resident blocks only (grid-stride loops over the rows)
+    int nb64 = 0, nbff = 0;
+    if ((st = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb64, k_cheb, 256, 0)) != cudaSuccess ||
+        (st = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nbff, k_cheb_ff, 256, 0)) != cudaSuccess)
+      return eig_fail(GM_ERR_CUDA, "deflation_pairs: occupancy: %s", cudaGetErrorString(st));
+    S.grid64 = (unsigned)std::max(1, nb64 * S.nsm);
+    S.grid_ff = (unsigned)std::max(1, nbff * S.nsm);
+  }
   if ((st = cudaMemcpy(S.rp, hrp.data(), sizeof(long long) * (n + 1), cudaMemcpyHostToDevice)) != cudaSuccess ||
       (st = cudaMemcpy(S.ci, hci.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice)) != cudaSuccess ||
       (st = cudaMemcpy(S.va, hva.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice)) != cudaSuccess)
@@ -416,6 +533,9 @@ extern "C" int gm_deflation_pairs(int64_t n, const int64_t* rowptr, const int32_
   double* Yn = S.buf[4];
   double* T = S.buf[5];   // scratch
   const unsigned ge = (unsigned)std::max(1, S.nsm * 8);
+  // float-float filter only where the values and the filter's intermediates
+  // stay well inside FP32's exponent range
+  bool use_ff = use_ff_arg && b < 1e30 && vmin > 1e-30;
   double theta[P] = {};
   double res[P] = {};
   int iters = 0, rc = GM_OK;
@@ -457,27 +577,58 @@ extern "C" int gm_deflation_pairs(int64_t n, const int64_t* rowptr, const int32_
     const double e = 0.5 * (b - a), c = 0.5 * (b + a);
     const double rate = std::acosh((c - a0) / e);
     const int deg = (int)std::min<double>(max_degree, std::max(4.0, std::ceil(std::log(kCondCap) / rate)));
-    // scaled Chebyshev filter (Zhou, Saad, Tiago, Chelikowsky, Algorithm 4.1)
+    // scaled Chebyshev filter (Zhou, Saad, Tiago, Chelikowsky, Algorithm 4.1).
+    // While the wanted residuals are far above kFFUntil it runs in float-float
+    // (about 48 bits, on the FP32 pipe); its rounding floors the reachable
+    // residual near 1e-7 on an operator with kappa ~ 1e7, so the last
+    // iterations, and every Rayleigh-Ritz step, are FP64.
     double sig = e / (a0 - c);
     const double tau = 2.0 / sig;
-    if (S.spmm_axpby(X, nullptr, Y, sig / e, -c * sig / e, 0.0) != cudaSuccess) rc = GM_ERR_CUDA;
-    double* prev = X;
-    for (int i = 2; i <= deg && rc == GM_OK; ++i) {
-      const double sig2 = 1.0 / (tau - sig);
-      if (S.spmm_axpby(Y, prev, Yn, 2.0 * sig2 / e, -2.0 * c * sig2 / e, -sig * sig2) != cudaSuccess) rc = GM_ERR_CUDA;
-      // rotate: prev <- Y, Y <- Yn (X is kept untouched after the first step)
-      double* old = prev == X ? Yp : prev;
-      prev = Y;
-      Y = Yn;
-      Yn = old;
-      sig = sig2;
+    const bool ff_now = use_ff && maxres > kFFUntil;
+    double* Yf = nullptr;   // the filtered block, FP64
+    if (ff_now) {
+      float2* pf = reinterpret_cast<float2*>(S.buf[3]);
+      float2* yf = reinterpret_cast<float2*>(S.buf[2]);
+      float2* nf = reinterpret_cast<float2*>(S.buf[4]);
+      k_d2ff<<<ge, 256>>>(n * P, X, pf);
+      if (S.spmm_axpby_ff(pf, nullptr, yf, sig / e, -c * sig / e, 0.0) != cudaSuccess) rc = GM_ERR_CUDA;
+      for (int i = 2; i <= deg && rc == GM_OK; ++i) {
+        const double sig2 = 1.0 / (tau - sig);
+        if (S.spmm_axpby_ff(yf, pf, nf, 2.0 * sig2 / e, -2.0 * c * sig2 / e, -sig * sig2) != cudaSuccess)
+          rc = GM_ERR_CUDA;
+        float2* old = pf;
+        pf = yf;
+        yf = nf;
+        nf = old;
+        sig = sig2;
+      }
+      Yf = yf == reinterpret_cast<float2*>(S.buf[2]) ? S.buf[3] : S.buf[2];
+      k_ff2d<<<ge, 256>>>(n * P, yf, Yf);
+    } else {
+      if (S.spmm_axpby(X, nullptr, Y, sig / e, -c * sig / e, 0.0) != cudaSuccess) rc = GM_ERR_CUDA;
+      double* prev = X;
+      for (int i = 2; i <= deg && rc == GM_OK; ++i) {
+        const double sig2 = 1.0 / (tau - sig);
+        if (S.spmm_axpby(Y, prev, Yn, 2.0 * sig2 / e, -2.0 * c * sig2 / e, -sig * sig2) != cudaSuccess)
+          rc = GM_ERR_CUDA;
+        // rotate: prev <- Y, Y <- Yn (X is kept untouched after the first step)
+        double* old = prev == X ? Yp : prev;
+        prev = Y;
+        Y = Yn;
+        Yn = old;
+        sig = sig2;
+      }
+      Yf = Y;
     }
     if (rc != GM_OK) {
       rc = eig_fail(GM_ERR_CUDA, "deflation_pairs: filter launch: %s", cudaGetErrorString(cudaGetLastError()));
       break;
     }
-    q = S.cholqr2(Y, T);
-    if (q == 0) q = rayleigh_ritz(Y);
+    const double res_before = maxres;
+    q = S.cholqr2(Yf, T);
+    if (q == 0) q = rayleigh_ritz(Yf);
+    // a float-float iteration that no longer halves the residual has met its floor
+    if (q == 0 && ff_now && maxres < 1e-3 && maxres > 0.5 * res_before) use_ff = false;
     if (q != 0) {
       rc = q < 0 ? eig_fail(GM_ERR_CUDA, "deflation_pairs: %s", cudaGetErrorString(cudaGetLastError()))
                  : eig_fail(GM_ERR_BREAKDOWN, "deflation_pairs: filtered block rank deficient (degree %d)", deg);
@@ -513,6 +664,7 @@ extern "C" int gm_deflation_pairs(int64_t n, const int64_t* rowptr, const int32_
     stats[5] = a;
     stats[6] = theta[P - 1];
     stats[7] = (double)nnz;
+    stats[8] = (double)S.spmm_ff;
   }
   return rc;
 }

@@ -19,13 +19,15 @@ __all__ = ["deflation_pairs", "MAX_K"]
 
 MAX_K = 24
 _STATS = ("iterations", "block_spmvs", "device_s", "max_rel_residual", "gershgorin_bound", "filter_cut",
-          "block_top_ritz", "nnz")
+          "block_top_ritz", "nnz", "block_spmvs_float_float")
 
 
 def deflation_pairs(A, k: int, tol: float = 1e-8, max_degree: int = 1000, max_iter: int = 200, seed: int = 0,
-                    raise_on_noconv: bool = True):
+                    raise_on_noconv: bool = True, float_float_filter: bool = True):
     """(lambda (k,), Q (n, k), stats dict) for the k smallest eigenpairs of the
-    symmetric sparse A, computed on the current CUDA device."""
+    symmetric sparse A, computed on the current CUDA device.  With
+    ``float_float_filter`` the early filter applications run in float-float
+    arithmetic on the FP32 pipe; otherwise every step is FP64."""
     lib = load_library()
     A = sp.csr_matrix(A)
     A.sort_indices()
@@ -35,9 +37,10 @@ def deflation_pairs(A, k: int, tol: float = 1e-8, max_degree: int = 1000, max_it
     va = np.ascontiguousarray(A.data, dtype=np.float64)
     lam = np.empty(k)
     Q = np.empty((n, k), order="F")
-    stats = (ct.c_double * 8)()
+    stats = (ct.c_double * 9)()
+    deg = int(max_degree) if float_float_filter else -int(max_degree)
     rc = lib.gm_deflation_pairs(n, rp.ctypes.data, ci.ctypes.data, va.ctypes.data, int(k), float(tol),
-                                int(max_degree), int(max_iter), int(seed), lam.ctypes.data, Q.ctypes.data, stats)
+                                deg, int(max_iter), int(seed), lam.ctypes.data, Q.ctypes.data, stats)
     info = dict(zip(_STATS, list(stats)))
     if rc != 0 and not (rc == 9 and not raise_on_noconv):
         raise GmError(rc, (lib.gm_last_error(None) or b"").decode())

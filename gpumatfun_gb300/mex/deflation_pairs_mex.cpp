@@ -5,7 +5,7 @@
  *   [lambda, Q] = deflation_pairs_mex(A, k)
  *   [lambda, Q, stats] = deflation_pairs_mex(A, k, tol, max_degree, max_iter, seed)
  * lambda is k x 1 ascending, Q is n x k with orthonormal columns; stats is the
- * 8-vector of gm_deflation_pairs. */
+ * 9-vector of gm_deflation_pairs. */
 #include <math.h>
 #include <vector>
 #include "gm_mex_common.h"
@@ -28,7 +28,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
     deg = mxGetScalar(prhs[3]);
     iters = mxGetScalar(prhs[4]);
     seed = mxGetScalar(prhs[5]);
-    if (deg != floor(deg) || iters != floor(iters) || seed != floor(seed) || !(seed >= 0) || deg > 1e9 || iters > 1e9)
+    if (deg != floor(deg) || iters != floor(iters) || seed != floor(seed) || !(seed >= 0) || fabs(deg) > 1e9 || iters > 1e9)
       mexErrMsgIdAndTxt("MATLAB:deflation_pairs:badOption", "max_degree, max_iter and seed must be whole numbers.");
   }
   const size_t n = mxGetN(A);
@@ -42,7 +42,7 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
   const int k = (int)kd;
   plhs[0] = mxCreateDoubleMatrix((mwSize)k, 1, mxREAL);
   mxArray* Q = mxCreateDoubleMatrix((mwSize)n, (mwSize)k, mxREAL);
-  mxArray* st = mxCreateDoubleMatrix(8, 1, mxREAL);
+  mxArray* st = mxCreateDoubleMatrix(9, 1, mxREAL);
   const int rc = gm_deflation_pairs((int64_t)n, ptr.data(), col.data(), mxGetPr(A), k, tol, (int)deg, (int)iters,
                                     (uint64_t)seed, mxGetPr(plhs[0]), mxGetPr(Q), mxGetPr(st));
   gm_mex_check(rc, nullptr, "deflation_pairs");

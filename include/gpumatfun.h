@@ -392,19 +392,22 @@ int gm_lin_sys_solves_noalloc(int m, int nrhs, int contour_size, const double* a
  * mass M this is the symmetric A = M^{-1/2} K M^{-1/2} the engine takes).
  *
  * Method: Chebyshev-filtered subspace iteration over a block of 32 vectors on
- * the GPU, all in FP64: scaled Chebyshev filter on [largest Ritz value,
- * Gershgorin bound], CholQR2, Rayleigh-Ritz with a Jacobi eigensolver of the
- * 32 x 32 projection.  1 <= k <= 24, n >= 64.  Iterates until every wanted
- * relative residual ||A q_j - lambda_j q_j|| / |lambda_j| <= tol, or for at
- * most max_iter filter applications of degree <= max_degree; seed fixes the
- * start block.  Outputs (host or device): lambda (k, ascending) and Q (n x k,
- * column-major, orthonormal columns).  stats (8 doubles, may be NULL):
- * [0] iterations, [1] block SpMVs, [2] device seconds, [3] largest wanted
- * relative residual, [4] Gershgorin bound, [5] last filter cut, [6] largest
- * Ritz value of the block, [7] nnz.  Returns GM_ERR_NOCONV (outputs and stats
- * still written) when the tolerance was not reached; messages in
- * gm_last_error(NULL).  Allocates about 6 n 256 + 12 nnz bytes of device
- * memory for the duration of the call and synchronises the device. */
+ * the GPU: scaled Chebyshev filter on [largest Ritz value, Gershgorin bound],
+ * CholQR2, Rayleigh-Ritz with a Jacobi eigensolver of the 32 x 32
+ * projection, all in FP64 except the filter while the wanted residuals are
+ * above 1e-7, which runs in float-float arithmetic (about 48 bits) on the
+ * FP32 pipe; a negative max_degree keeps the filter in FP64 throughout.
+ * 1 <= k <= 24, n >= 64.  Iterates until every wanted relative residual
+ * ||A q_j - lambda_j q_j|| / |lambda_j| <= tol, or for at most max_iter
+ * filter applications of degree <= |max_degree|; seed fixes the start block.
+ * Outputs (host or device): lambda (k, ascending) and Q (n x k, column-major,
+ * orthonormal columns).  stats (9 doubles, may be NULL): [0] iterations,
+ * [1] block SpMVs, [2] device seconds, [3] largest wanted relative residual,
+ * [4] Gershgorin bound, [5] last filter cut, [6] largest Ritz value of the
+ * block, [7] nnz, [8] block SpMVs in float-float.  Returns GM_ERR_NOCONV
+ * (outputs and stats still written) when the tolerance was not reached;
+ * messages in gm_last_error(NULL).  Allocates about 6 n 256 + 20 nnz bytes of
+ * device memory for the duration of the call and synchronises the device. */
 int gm_deflation_pairs(int64_t n, const int64_t* rowptr, const int32_t* col, const double* val, int k,
                        double tol, int max_degree, int max_iter, uint64_t seed, double* lambda, double* Q,
                        double* stats);

@@ -59,10 +59,12 @@ def test_fe_disk_against_eigsh(engine_lib):
     lam_ref, Q_ref = sla.eigsh(A, k=k, sigma=0.0, which="LM", OPinv=op, tol=1e-12)
     o = np.argsort(lam_ref)
     lam_ref, Q_ref = lam_ref[o], Q_ref[:, o]
-    lam, Q, st = eigs.deflation_pairs(A, k)
-    np.testing.assert_allclose(lam, lam_ref, rtol=1e-10)
-    assert rel_residuals(A, lam, Q).max() <= 1e-8
-    assert subspace_cos_min(Q_ref, Q) > 1 - 1e-10
+    for ff in (True, False):   # float-float filter until 1e-7, then FP64; or FP64 throughout
+        lam, Q, st = eigs.deflation_pairs(A, k, float_float_filter=ff)
+        assert (st["block_spmvs_float_float"] > 0) == ff
+        np.testing.assert_allclose(lam, lam_ref, rtol=1e-10)
+        assert rel_residuals(A, lam, Q).max() <= 1e-8
+        assert subspace_cos_min(Q_ref, Q) > 1 - 1e-10
 
 
 def test_fe_disk_1M_against_eigsh_and_in_the_engine(engine_lib):
@@ -71,7 +73,8 @@ def test_fe_disk_1M_against_eigsh_and_in_the_engine(engine_lib):
     P = workloads.cached_problem("fe-disk-1M", R=1)
     lam, Q, st = eigs.deflation_pairs(P.A, P.k)
     print(f"1M disk GPU deflation pairs: {st['iterations']:.0f} iterations, {st['block_spmvs']:.0f} block "
-          f"SpMVs, {st['device_s']:.2f} s, max rel residual {st['max_rel_residual']:.2e}")
+          f"SpMVs ({st['block_spmvs_float_float']:.0f} float-float), {st['device_s']:.2f} s, "
+          f"max rel residual {st['max_rel_residual']:.2e}")
     assert st["converged"]
     err = np.max(np.abs(lam - P.lam) / P.lam)
     assert err <= 1e-8, err
