@@ -52,8 +52,9 @@ def parse():
     ap.add_argument("--max-blocks", type=int, default=0, help="cap on the grid size (0: engine default)")
     ap.add_argument("--diag-compensation", type=int, default=0, choices=[0, 1],
                     help="mixed engine: 0 = diagonal-compensated FP32 matrix, 1 = plain FP32 values")
-    ap.add_argument("--col-staging", type=int, default=0, choices=[0, 1],
-                    help="0: stage SELL column indices in shared memory by TMA, 1: off")
+    ap.add_argument("--col-staging", type=int, default=0, choices=[0, 1, 2],
+                    help="SELL column indices staged in shared memory by TMA: 0 auto (when the matrix is "
+                         "not held in L2), 1 off, 2 on")
     ap.add_argument("--matrix-powers", type=int, default=None, choices=[0, 1],
                     help="1: two Horner levels of the polynomial per SpMV pass "
                          "(default: off for the f(A)b workloads, on for the adjoint)")
@@ -671,7 +672,7 @@ def _timed_solves(eng, stream, K, W):
 # Launch shape of the batch when it is not autotuned: the one the autotuner
 # chose on GB300 for both precisions (256-thread blocks, grid barriers
 # between passes, column staging on, residency from the occupancy limit).
-BATCH_SHAPE = dict(threads=256, blocks_per_sm=0, col_staging=0, sync_policy=1)
+BATCH_SHAPE = dict(threads=256, blocks_per_sm=0, col_staging=2, sync_policy=1)
 
 
 def batch_measure(K: int, W: int, tune: bool, monodomain: bool = True) -> dict:
@@ -698,7 +699,7 @@ def batch_measure(K: int, W: int, tune: bool, monodomain: bool = True) -> dict:
             t = autotune.tune_batch(probs, precision=prec, reps=2, device=torch.cuda.get_device_name())
             shape = {k: t[k] for k in ("threads", "blocks_per_sm", "col_staging", "sync_policy")}
             default = [c for c in t.get("timed", []) if c["threads"] == 512 and c["blocks_per_sm"] == 0
-                       and c["col_staging"] == 0 and c["sync_policy"] == 0]
+                       and c["col_staging"] == 2 and c["sync_policy"] == 0]
             shapes[prec] = dict(shape, tuned_ms=t["ms"], default_shape_ms=default[0]["ms"] if default else None,
                                 cached=t["cached"], candidates=t["trials"])
         else:

@@ -42,7 +42,7 @@ def signature(P, precision: str, device: str = "") -> str:
     hist = np.bincount(np.minimum(lens, 32), minlength=33)
     frac = np.round(hist / max(1, lens.size), 3).tolist()
     key = dict(n=int(P.n), nnz=int(P.A.nnz), rowlen=frac, R=int(P.R), m=int(P.m), d=int(P.d), C=int(P.C),
-               precision=str(precision), device=device)
+               precision=str(precision), device=device, space=2)
     return hashlib.sha1(json.dumps(key, sort_keys=True).encode()).hexdigest()[:16]
 
 
@@ -53,7 +53,7 @@ def candidates(R: int, degree: int = 0, ragged: bool = False) -> list:
     threads = (128, 256, 512)
     bps = (0, 1) if R >= 4 else (0, 1, 2)
     out = []
-    for t, b, stg, pol in itertools.product(threads, bps, (0, 1), (0, 1)):
+    for t, b, stg, pol in itertools.product(threads, bps, (1, 2), (0, 1)):
         out.append(dict(threads=t, blocks_per_sm=b, col_staging=stg, sync_policy=pol, matrix_powers=0, sell_sigma=0))
         if degree >= 2 and pol == 0:
             out.append(dict(threads=t, blocks_per_sm=b, col_staging=stg, sync_policy=pol, matrix_powers=1,
@@ -145,7 +145,7 @@ def batch_signature(problems, precision: str, device: str = "") -> str:
     nrhs, m, d, C and the precision."""
     P0 = problems[0]
     key = dict(sizes=[[int(P.n), int(P.A.nnz)] for P in problems], R=int(P0.R), m=int(P0.m), d=int(P0.d),
-               C=int(P0.C), precision=str(precision), device=device, batch=True)
+               C=int(P0.C), precision=str(precision), device=device, batch=True, space=2)
     return hashlib.sha1(json.dumps(key, sort_keys=True).encode()).hexdigest()[:16]
 
 
@@ -154,7 +154,7 @@ def batch_candidates(R: int) -> list:
     and pass ordering (each problem keeps its own barrier)."""
     bps = (0, 1) if R >= 4 else (0, 1, 2)
     return [dict(threads=t, blocks_per_sm=b, col_staging=stg, sync_policy=pol)
-            for t, b, stg, pol in itertools.product((256, 512), bps, (0, 1), (0, 1))]
+            for t, b, stg, pol in itertools.product((256, 512), bps, (1, 2), (0, 1))]
 
 
 def _measure_batch(problems, precision: str, reps: int) -> Callable[[dict], float]:

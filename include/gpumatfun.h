@@ -109,8 +109,11 @@ typedef struct gm_create_args {
   int sync_policy;             /* ordering of consecutive SpMV passes: 0 = waits on
                                   the blocks owning referenced rows (default),
                                   1 = grid barriers                               */
-  int col_staging;             /* 0 = stage SELL column indices in shared memory by
-                                  TMA bulk copies (default), 1 = read them directly */
+  int col_staging;             /* SELL column indices staged in shared memory by TMA
+                                  bulk copies (with the value prefetch): 0 = when
+                                  the matrix is not held in the L2 window or
+                                  val_prefetch = 1 (default), 1 = never (read
+                                  directly), 2 = always                            */
   int keep_entry_map;          /* 1 = keep the map from stored entries (CSR order)
                                   to device slots, needed by gm_fe_attach          */
   int l2_window;               /* 0 = launches keep the SELL matrix resident in L2

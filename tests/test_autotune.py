@@ -14,7 +14,7 @@ def test_tune_picks_fastest_and_caches(tmp_path):
 
     path = tmp_path / "tune.json"
     r = autotune.tune(P, "mixed", cache_path=str(path), measure=fake)
-    assert r["threads"] == 256 and r["col_staging"] == 0 and r["sync_policy"] == 0 and r["blocks_per_sm"] == 0
+    assert r["threads"] == 256 and r["col_staging"] == 1 and r["sync_policy"] == 0 and r["blocks_per_sm"] == 0
     assert not r["cached"] and r["trials"] == len(autotune.candidates(2)) == len(calls)
     r2 = autotune.tune(P, "mixed", cache_path=str(path), measure=fake)
     assert r2["cached"] and len(calls) == r["trials"]

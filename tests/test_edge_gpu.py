@@ -110,7 +110,7 @@ def test_batch_with_zero_column(engine_lib):
 
 def test_autotune_on_gpu(engine_lib, tmp_path):
     P = workloads.config1_small(N=40, k=0, m=20, C=16, R=1)
-    space = [dict(threads=256, blocks_per_sm=0, col_staging=0, sync_policy=0),
+    space = [dict(threads=256, blocks_per_sm=0, col_staging=2, sync_policy=0),
              dict(threads=128, blocks_per_sm=0, col_staging=1, sync_policy=1)]
     cache = tmp_path / "tune.json"
     best = autotune.tune(P, precision="fp64", reps=2, cache_path=str(cache), space=space)

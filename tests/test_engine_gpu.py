@@ -261,8 +261,9 @@ def test_zero_rhs(engine_lib):
 
 @pytest.mark.parametrize("degree", [0, 3, 6])
 def test_sync_policies_agree(engine_lib, degree):
-    """Neighbour waits between SpMV passes (default) and grid barriers give
-    the same bits: the passes compute identical values in identical order.
+    """Neighbour waits between SpMV passes (default) and grid barriers, with
+    the SELL column indices staged in shared memory by TMA or read directly,
+    give the same bits: the passes compute identical values in identical order.
     The grid is large (hundreds of blocks, several Horner passes in both the
     Lanczos and the apply phase) so that an ordering race would show."""
     N = 180
@@ -270,8 +271,8 @@ def test_sync_policies_agree(engine_lib, degree):
                                seed=2, degree=degree)
     want = oracle_for(P).solve()
     out = []
-    for pol in (0, 1):
-        eng = Engine.from_problem(P, sync_policy=pol, threads=128, sync=False)
+    for pol, stg in ((0, 1), (1, 1), (0, 2), (1, 2)):   # and column staging off / on
+        eng = Engine.from_problem(P, sync_policy=pol, threads=128, sync=False, col_staging=stg)
         assert eng.info()["grid_blocks"] > 200
         for _ in range(3):
             eng.solve()
