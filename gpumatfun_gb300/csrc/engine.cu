@@ -877,10 +877,13 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
   // Column staging: per warp two stages of stage_cap * 32 column indices
   // (slices with more columns are read from global memory directly), with
   // the value prefetch riding on each stage's copy.  It pays for a matrix
-  // streamed from HBM; for a matrix held in the L2 window it only adds work
-  // (measured on the 1M-node FE disk, one right-hand side: FP64 22.38 vs
-  // 21.83 ms per solve, mixed 17.95 vs 16.29 ms, with staging on vs off), so
-  // by default it is on only when the window is not used.
+  // streamed from HBM (3D 256^3: mixed 56.7 vs 51.8 ms per solve without vs
+  // with staging; the 1M-node FE disk with four right-hand sides, whose
+  // vectors push the matrix out of L2: 58.4 vs 49.7 ms); for a matrix held in
+  // the L2 window it only adds work (the same disk with one right-hand side:
+  // mixed 18.2 vs 16.8 ms with vs without, FP64 equal within 0.5%; the 250k
+  // adjoint 317 vs 310 ms per gradient), so by default it is on only when the
+  // window is not used.
   if (a->col_staging < 0 || a->col_staging > 2) return fail(e, GM_ERR_ARG, "col_staging must be 0 (auto), 1 (off) or 2 (on)");
   long long max_len = 0;
   for (size_t q = 0; q + 1 < slice_off.size(); ++q) max_len = std::max(max_len, (slice_off[q + 1] - slice_off[q]) / 32);
