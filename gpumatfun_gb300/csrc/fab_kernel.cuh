@@ -195,9 +195,14 @@ __device__ __forceinline__ long long slot_row(const KParams& kp, long long s, in
 // x are issued, then the CH products are accumulated, so each chunk costs two
 // memory latencies instead of 2*CH.
 // Chunk width: one column index, one value and R gathered entries are live
-// per chunk element across the gathers.  These widths are the largest that
-// compile without local-memory spills at the kernel's 128-register bound
-// (checked with -Xptxas -v for every instantiation).
+// per chunk element across the gathers.  For R = 1, 2 these are the largest
+// widths that compile without local-memory spills at the 64-register bound of
+// two 512-thread blocks per SM (checked with -Xptxas -v for every
+// instantiation).  For R = 4 the kernels also run two blocks per SM
+// (GM_MINB4), where one entry per chunk is what fits: twice the resident
+// warps with one gather each beat one block per SM with three gathers each
+// at 128 registers (1M-node FE disk, four right-hand sides: mixed 39.96 vs
+// 48.66 ms per launch, FP64 58.6 vs 64.9 ms).
 #ifndef GM_CH1
 #define GM_CH1 4
 #endif
@@ -205,10 +210,10 @@ __device__ __forceinline__ long long slot_row(const KParams& kp, long long s, in
 #define GM_CH2 2
 #endif
 #ifndef GM_CH4
-#define GM_CH4 2
+#define GM_CH4 1
 #endif
 #ifndef GM_CH4F
-#define GM_CH4F 3
+#define GM_CH4F 1
 #endif
 template <class VT, class XT, int R>
 struct ChunkWidth {
@@ -1341,7 +1346,10 @@ template <class Pol, int R, int PH>
 #ifndef GM_MAXT
 #define GM_MAXT 512
 #endif
-__global__ void __launch_bounds__(GM_MAXT, (R >= 4 ? 1 : GM_MINB)) fab_kernel(KParams kp) {
+#ifndef GM_MINB4
+#define GM_MINB4 2   // resident 512-thread blocks per SM for four right-hand sides
+#endif
+__global__ void __launch_bounds__(GM_MAXT, (R >= 4 ? GM_MINB4 : GM_MINB)) fab_kernel(KParams kp) {
   const Ctx c(kp.G);
   if (*(volatile int*)kp.status != 0) return;
   const int ph = kp.phases & PH;
