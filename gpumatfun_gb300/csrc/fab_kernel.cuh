@@ -195,16 +195,22 @@ __device__ __forceinline__ long long slot_row(const KParams& kp, long long s, in
 // x are issued, then the CH products are accumulated, so each chunk costs two
 // memory latencies instead of 2*CH.
 // Chunk width: one column index, one value and R gathered entries are live
-// per chunk element across the gathers.  For R = 1, 2 these are the largest
-// widths that compile without local-memory spills at the 64-register bound of
-// two 512-thread blocks per SM (checked with -Xptxas -v for every
-// instantiation).  For R = 4 the kernels also run two blocks per SM
-// (GM_MINB4), where one entry per chunk is what fits: twice the resident
-// warps with one gather each beat one block per SM with three gathers each
-// at 128 registers (1M-node FE disk, four right-hand sides: mixed 39.96 vs
-// 48.66 ms per launch, FP64 58.6 vs 64.9 ms).
+// per chunk element across the gathers.  What the SpMV needs is loads in
+// flight per SM, and resident warps supply them more cheaply than wide
+// chunks: every right-hand-side count runs its kernels at the residency
+// below with the chunk width that fits it.
+//   R = 1: three 512-thread blocks per SM (GM_MINB1, 42 registers), one entry
+//          per chunk; against two blocks with four entries: 3D 256^3 mixed
+//          40.6 vs 51.0 ms per solve, FP64 50.0 vs 63.6 ms, 1M-node FE disk
+//          FP64 21.2 vs 22.1 ms, mixed equal (16.5 ms), despite the spills at
+//          42 registers.
+//   R = 2: two blocks per SM (GM_MINB, 64 registers), two entries per chunk,
+//          the widest without spills there.
+//   R = 4: two blocks per SM (GM_MINB4), one entry per chunk; against one
+//          block with three entries at 128 registers (1M-node FE disk: mixed
+//          40.0 vs 48.7 ms per launch, FP64 58.6 vs 64.9 ms).
 #ifndef GM_CH1
-#define GM_CH1 4
+#define GM_CH1 1
 #endif
 #ifndef GM_CH2
 #define GM_CH2 2
@@ -1349,7 +1355,10 @@ template <class Pol, int R, int PH>
 #ifndef GM_MINB4
 #define GM_MINB4 2   // resident 512-thread blocks per SM for four right-hand sides
 #endif
-__global__ void __launch_bounds__(GM_MAXT, (R >= 4 ? GM_MINB4 : GM_MINB)) fab_kernel(KParams kp) {
+#ifndef GM_MINB1
+#define GM_MINB1 3   // and for one right-hand side
+#endif
+__global__ void __launch_bounds__(GM_MAXT, (R >= 4 ? GM_MINB4 : (R == 1 ? GM_MINB1 : GM_MINB))) fab_kernel(KParams kp) {
   const Ctx c(kp.G);
   if (*(volatile int*)kp.status != 0) return;
   const int ph = kp.phases & PH;
