@@ -203,7 +203,9 @@ __device__ __forceinline__ long long slot_row(const KParams& kp, long long s, in
 //          per chunk; against two blocks with four entries: 3D 256^3 mixed
 //          40.6 vs 51.0 ms per solve, FP64 50.0 vs 63.6 ms, 1M-node FE disk
 //          FP64 21.2 vs 22.1 ms, mixed equal (16.5 ms), despite the spills at
-//          42 registers.
+//          42 registers.  The matrix-powers and Gram-Schmidt entry points,
+//          whose passes hold more state, stay at two blocks (GM_MINB1X): the
+//          250k-node adjoint 288 vs 325 ms per gradient with three.
 //   R = 2: two blocks per SM (GM_MINB, 64 registers), two entries per chunk,
 //          the widest without spills there.
 //   R = 4: two blocks per SM (GM_MINB4), one entry per chunk; against one
@@ -1358,7 +1360,12 @@ template <class Pol, int R, int PH>
 #ifndef GM_MINB1
 #define GM_MINB1 3   // and for one right-hand side
 #endif
-__global__ void __launch_bounds__(GM_MAXT, (R >= 4 ? GM_MINB4 : (R == 1 ? GM_MINB1 : GM_MINB))) fab_kernel(KParams kp) {
+#ifndef GM_MINB1X
+#define GM_MINB1X 2   // one right-hand side, matrix-powers or Gram-Schmidt entry points
+#endif
+__global__ void __launch_bounds__(GM_MAXT, (R >= 4 ? GM_MINB4
+                                            : (R == 1 ? ((PH & (PH_MPK | PH_REORTH)) ? GM_MINB1X : GM_MINB1)
+                                                      : GM_MINB))) fab_kernel(KParams kp) {
   const Ctx c(kp.G);
   if (*(volatile int*)kp.status != 0) return;
   const int ph = kp.phases & PH;
