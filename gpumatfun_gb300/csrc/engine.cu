@@ -897,8 +897,10 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
     if (a->val_prefetch == 1 || !use_window) e->kp.pf_vals = e->prec == GM_FP64 ? 8 : 4;
   }
   // Grid: blocks_per_sm x SMs, capped by co-residency of each phase-group
-  // kernel and by the work (about one SELL slice per warp: small problems
-  // get fewer blocks, which makes every grid barrier cheaper).
+  // kernel this engine can launch and by the work (about one SELL slice per
+  // warp: small problems get fewer blocks, which makes every grid barrier
+  // cheaper).  The matrix-powers and Gram-Schmidt groups, compiled for fewer
+  // resident blocks, bound the grid only of engines that launch them.
   const long long nsl = (long long)slice_off.size() - 1;
   const int nw = e->threads / 32;
   const long long want = std::max<long long>(np, (nsl + nw - 1) / nw);
@@ -910,6 +912,12 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
                   g == KGRP_FUSED_MPK || g == KGRP_LANCZOS_RO || g == KGRP_FUSED_RO) ? stage_smem : 0;
     if (e->smem[g] > 48 * 1024)
       GM_CUDA(e, raise_smem_limit(e->dev, e->kfn[g], e->smem[g]));
+    const bool ro_grp = g == KGRP_LANCZOS_RO || g == KGRP_FUSED_RO;
+    const bool mpk_grp = g == KGRP_LANCZOS_MPK || g == KGRP_FUSED_MPK;
+    if ((ro_grp && a->reorth == 0) || (mpk_grp && !e->mpk_req)) {
+      e->Gk[g] = 0;   // never launched
+      continue;
+    }
     int nb = 0;
     GM_CUDA(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, e->kfn[g], e->threads, e->smem[g]));
     if (nb < 1) return fail(e, GM_ERR_UNSUPPORTED, "kernel group %d cannot be resident with %d threads", g, e->threads);

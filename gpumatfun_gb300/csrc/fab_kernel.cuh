@@ -210,7 +210,10 @@ __device__ __forceinline__ long long slot_row(const KParams& kp, long long s, in
 //          the widest without spills there.
 //   R = 4: two blocks per SM (GM_MINB4), one entry per chunk; against one
 //          block with three entries at 128 registers (1M-node FE disk: mixed
-//          40.0 vs 48.7 ms per launch, FP64 58.6 vs 64.9 ms).
+//          40.0 vs 48.7 ms per launch, FP64 58.6 vs 64.9 ms).  The mixed
+//          policy's Lanczos entry points run three blocks (GM_MINB4M): 1M-node
+//          disk 39.0 vs 40.5 ms, 64-problem batch 19.0 vs 20.3 ms, where FP64
+//          at three blocks is slower (63.1 vs 58.8 ms).
 #ifndef GM_CH1
 #define GM_CH1 1
 #endif
@@ -1357,13 +1360,16 @@ template <class Pol, int R, int PH>
 #ifndef GM_MINB4
 #define GM_MINB4 2   // resident 512-thread blocks per SM for four right-hand sides
 #endif
+#ifndef GM_MINB4M
+#define GM_MINB4M 3   // four right-hand sides, mixed precision, Lanczos entry points
+#endif
 #ifndef GM_MINB1
 #define GM_MINB1 3   // and for one right-hand side
 #endif
 #ifndef GM_MINB1X
 #define GM_MINB1X 2   // one right-hand side, matrix-powers or Gram-Schmidt entry points
 #endif
-__global__ void __launch_bounds__(GM_MAXT, (R >= 4 ? GM_MINB4
+__global__ void __launch_bounds__(GM_MAXT, (R >= 4 ? ((Pol::kMixed && !(PH & (PH_MPK | PH_REORTH))) ? GM_MINB4M : GM_MINB4)
                                             : (R == 1 ? ((PH & (PH_MPK | PH_REORTH)) ? GM_MINB1X : GM_MINB1)
                                                       : GM_MINB))) fab_kernel(KParams kp) {
   const Ctx c(kp.G);
