@@ -358,9 +358,12 @@ def run_ours(args, P, rank, world, local):
             "peak_kind": f"{peak_kind} copy bandwidth (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
             else "fallback 6.8 TB/s", "traffic": traffic, "algorithmic_bytes_per_launch": alg,
             "ms_per_launch": ms_fused,
-            "frac_kind": "effective: algorithmic bytes over the launch time; the SELL matrix is served from "
-                         "the L2 persisting window on every pass after the first, so DRAM moves fewer bytes "
-                         "(dram_frac)",
+            "frac_kind": ("effective: algorithmic bytes over the launch time; the SELL matrix is served from "
+                          "the L2 persisting window on every pass after the first, so DRAM moves fewer bytes "
+                          "(dram_frac)") if info["l2_window_bytes"] else
+                         ("algorithmic bytes over the launch time; no L2 window: the SELL matrix streams from "
+                          "HBM on every pass (column staging, value prefetch)"),
+            "l2_window_bytes": info["l2_window_bytes"],
             "dram_achieved": traffic / (ms_fused * 1e-3) / 1e9 if traffic else None,
             "dram_frac": traffic / (ms_fused * 1e-3) / 1e9 / peak if traffic else None,
             "fp64_tflops": roofline.fused_solve_flops(sizes) / (ms_fused * 1e-3) / 1e12}
@@ -827,7 +830,8 @@ def fd3d_measure(N: int, K: int, W: int) -> dict:
                      "achieved_gb_s": ach, "peak_gb_s": peak, "frac": ach / peak,
                      "traffic": traffic,
                      "dram_frac": (traffic / (ms * 1e-3) / 1e9 / peak) if traffic else None,
-                     "grid_blocks": info["grid_blocks"], "value_prefetch_bytes": info["value_prefetch_bytes"]}
+                     "grid_blocks": info["grid_blocks"], "value_prefetch_bytes": info["value_prefetch_bytes"],
+                     "l2_window_bytes": info["l2_window_bytes"], "col_stage_groups": info["col_stage_groups"]}
     out["mixed_rel_err_vs_fp64_engine"] = float(np.linalg.norm(xs["mixed"] - xs["fp64"]) / np.linalg.norm(xs["fp64"]))
     out["mixed_over_fp64"] = out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"]
     out["setup_s"] = setup_s

@@ -1739,6 +1739,17 @@ int gm_info(gm_handle h, int64_t* info) {
   return GM_OK;
 }
 
+int gm_info_ex(gm_handle h, int64_t* info, int count) {
+  if (!h || !info || count < 0) return GM_ERR_ARG;
+  int64_t v[GM_INFO_EX_COUNT];
+  if (int rc = gm_info(h, v)) return rc;
+  v[16] = h->l2_window ? (int64_t)h->window.num_bytes : 0;
+  v[17] = h->kp.stage_cap;
+  v[18] = h->kp.dep_mode;
+  for (int i = 0; i < count && i < GM_INFO_EX_COUNT; ++i) info[i] = v[i];
+  return GM_OK;
+}
+
 const char* gm_last_error(gm_handle h) {
   return h ? h->err.c_str() : g_create_error.c_str();
 }

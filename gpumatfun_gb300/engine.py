@@ -32,7 +32,7 @@ EXPORTED_SYMBOLS = [
     "gm_lin_sys_solves", "gm_apply_V", "gm_update_U", "gm_update_U_monodomain", "gm_get_U",
     "gm_get_xsol", "gm_get_aabb", "gm_set_y", "gm_get_y", "gm_set_U", "gm_set_U_device", "gm_get_update",
     "gm_get_solution", "gm_solve", "gm_solve_host", "gm_sync", "gm_set_stream",
-    "gm_phase_times", "gm_info", "gm_get_meff", "gm_last_error", "gm_version",
+    "gm_phase_times", "gm_info", "gm_info_ex", "gm_get_meff", "gm_last_error", "gm_version",
     "gm_lin_sys_solves_noalloc", "gm_batch_create", "gm_time_loop", "gm_fe_attach", "gm_fe_assemble",
     "gm_fe_gradient", "gm_get_solution_device", "gm_fe_forward", "gm_fe_backward",
     "gm_fe_backward_stored", "gm_get_basis", "gm_get_ode", "gm_set_state", "gm_deflation_pairs",
@@ -120,6 +120,7 @@ def load_library(build_if_missing: bool = False) -> ct.CDLL:
     lib.gm_fe_backward_stored.argtypes = [h, ct.c_void_p, ct.c_void_p, ct.c_void_p]
     lib.gm_phase_times.argtypes = [h, ct.POINTER(ct.c_float)]
     lib.gm_info.argtypes = [h, _lp]
+    lib.gm_info_ex.argtypes = [h, _lp, ct.c_int]
     lib.gm_get_meff.argtypes = [h, ct.POINTER(ct.c_int)]
     lib.gm_deflation_pairs.argtypes = [ct.c_int64, ct.c_void_p, ct.c_void_p, ct.c_void_p, ct.c_int, ct.c_double,
                                        ct.c_int, ct.c_int, ct.c_uint64, ct.c_void_p, ct.c_void_p, _dp]
@@ -397,11 +398,12 @@ class Engine:
     nprob = 1
 
     def info(self) -> dict:
-        v = (ct.c_int64 * 16)()
-        self._check(self._lib.gm_info(self._h, v))
         keys = ("n", "nrhs", "m", "d", "C", "k", "precision", "grid_blocks", "threads",
                 "sell_padded", "device_bytes", "launches", "problems", "matrix_powers",
-                "value_prefetch_bytes", "reorth")
+                "value_prefetch_bytes", "reorth", "l2_window_bytes", "col_stage_groups",
+                "neighbour_waits")
+        v = (ct.c_int64 * len(keys))()
+        self._check(self._lib.gm_info_ex(self._h, v, len(keys)))
         return dict(zip(keys, list(v)))
 
     def meff(self) -> list:

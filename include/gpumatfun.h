@@ -351,6 +351,15 @@ int gm_phase_times(gm_handle h, float* ms5);
  * Lanczos step.  info has 16 entries. */
 int gm_info(gm_handle h, int64_t* info16);
 
+/* gm_info's entries followed by: [16] bytes of the matrix under the L2
+ * persisting access-policy window (0: no window, the matrix streams from
+ * HBM on every pass), [17] column-index staging depth in 32-column groups
+ * per stage (0: staging off), [18] 1 when passes wait on their neighbour
+ * blocks only, 0 when every pass ends at a grid barrier.  Fills the first
+ * min(count, GM_INFO_EX_COUNT) entries. */
+#define GM_INFO_EX_COUNT 19
+int gm_info_ex(gm_handle h, int64_t* info, int count);
+
 /* Effective Krylov dimension per (problem, RHS) after the last build (< m
  * after a breakdown). */
 int gm_get_meff(gm_handle h, int* meff);

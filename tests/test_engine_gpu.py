@@ -273,7 +273,10 @@ def test_sync_policies_agree(engine_lib, degree):
     out = []
     for pol, stg in ((0, 1), (1, 1), (0, 2), (1, 2)):   # and column staging off / on
         eng = Engine.from_problem(P, sync_policy=pol, threads=128, sync=False, col_staging=stg)
-        assert eng.info()["grid_blocks"] > 200
+        info = eng.info()
+        assert info["grid_blocks"] > 200
+        assert info["neighbour_waits"] == (1 if pol == 0 else 0)
+        assert (info["col_stage_groups"] > 0) == (stg == 2)
         for _ in range(3):
             eng.solve()
             out.append(eng.get_solution())
@@ -284,6 +287,28 @@ def test_sync_policies_agree(engine_lib, degree):
     for x in out[1:]:
         np.testing.assert_array_equal(x, out[0])
     assert rel(out[0], want) < FP64_TOL
+
+
+def test_info_ex_reports_l2_window_and_staging(engine_lib):
+    """gm_info_ex: the L2 window and the column staging each engine chose
+    (auto: window when the matrix and one pass's vectors fit L2, staging only
+    without a window), and a count below the total fills only that many."""
+    import ctypes as ct
+    P = workloads.fd2d_problem(64, 2, 24, 24, [params.frac_exp(1e-3, 1.5)], R=1, scale=65.0 ** 2, seed=3)
+    mat_bytes = 8 * P.A.nnz
+    for win, stg in ((0, 0), (1, 0), (2, 0), (1, 2)):
+        eng = Engine.from_problem(P, l2_window=win, col_staging=stg)
+        info = eng.info()
+        if win == 1:
+            assert info["l2_window_bytes"] == 0
+            assert (info["col_stage_groups"] > 0) == (stg in (0, 2))
+        else:
+            assert info["l2_window_bytes"] >= mat_bytes
+            assert info["col_stage_groups"] == 0
+        v = (ct.c_int64 * 19)(*([-7] * 19))
+        assert engine_lib.gm_info_ex(eng._h, v, 3) == 0
+        assert list(v)[:3] == [P.n, 1, P.m] and list(v)[3:] == [-7] * 16
+        eng.delete()
 
 
 def test_no_deflation_and_sigma_sorted(engine_lib):
