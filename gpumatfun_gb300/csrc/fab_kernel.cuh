@@ -241,6 +241,38 @@ __device__ __forceinline__ void acc_first(typename Pol::AT (&acc)[R], const type
     for (int r = 0; r < R; ++r) acc[r] = Pol::acc(acc[r], aa[u], xv[u][r]);
 }
 
+// One entry per step over a slice row: column index, value, gather, product.
+// The column source (shared-memory stage or global memory) is fixed for the
+// whole row, addresses advance by a slot column (32 entries) per step, and the
+// mixed engine's diagonal compensation (entry 0 is the diagonal) is peeled
+// out of the loop: the kernel is issue-bound, and these are the per-entry
+// instructions that are not the product itself.
+template <class Pol, int R, class XT, bool kStaged>
+__device__ __forceinline__ void row_entries1(const int* __restrict__ cp, const typename Pol::VT* __restrict__ vp,
+                                             int len, const XT* __restrict__ x, float dl,
+                                             typename Pol::AT (&acc)[R]) {
+  if (len <= 0) return;
+  XT xv[R];
+  int cc = kStaged ? cp[0] : __ldg(cp);
+  typename Pol::VT a = ld_val(vp);
+  VecIO<R>::ld(x + (long long)cc * R, xv);
+  if constexpr (Pol::kMixed) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[r] = Pol::acc(acc[r], dl, xv[r]);
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) acc[r] = Pol::acc(acc[r], a, xv[r]);
+  for (int jj = 1; jj < len; ++jj) {
+    cp += 32;
+    vp += 32;
+    cc = kStaged ? cp[0] : __ldg(cp);
+    a = ld_val(vp);
+    VecIO<R>::ld(x + (long long)cc * R, xv);
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[r] = Pol::acc(acc[r], a, xv[r]);
+  }
+}
+
 template <class Pol, int R, class XT>
 __device__ __forceinline__ void spmv_slot(const KParams& kp, long long s, int lane, const XT* __restrict__ x,
                                           typename Pol::AT (&acc)[R], const int* scol = nullptr,
@@ -249,6 +281,21 @@ __device__ __forceinline__ void spmv_slot(const KParams& kp, long long s, int la
   constexpr int CH = ChunkWidth<VT, XT, R>::value;
   const long long base = kp.slice_off[s];
   const int len = (int)((kp.slice_off[s + 1] - base) >> 5);
+  if constexpr (CH == 1) {
+    // same products in the same order as the chunked loop below
+#pragma unroll
+    for (int r = 0; r < R; ++r) acc[r] = Pol::zero();
+    float dl = 0.f;
+    if constexpr (Pol::kMixed) {
+      if (kp.dlo) dl = __ldg(kp.dlo + s * 32 + lane);
+    }
+    const VT* vp = reinterpret_cast<const VT*>(kp.val) + base + lane;
+    if (scol)
+      row_entries1<Pol, R, XT, true>(scol + lane, vp, len, x, dl, acc);
+    else
+      row_entries1<Pol, R, XT, false>((colarr ? colarr : kp.col) + base + lane, vp, len, x, dl, acc);
+    return;
+  }
   // Column indices from the shared-memory stage when the slice is staged,
   // else from global memory, chosen by a warp-uniform branch per chunk;
   // values from global memory (read-only path; with value prefetch they are
@@ -280,7 +327,7 @@ __device__ __forceinline__ void spmv_slot(const KParams& kp, long long s, int la
       for (int u = 0; u < CH; ++u) cc[u] = jj + u < len ? __ldg(gcp + (long long)(jj + u) * 32) : 0;
     }
 #pragma unroll
-    for (int u = 0; u < CH; ++u) aa[u] = jj + u < len ? __ldg(vp + (long long)(jj + u) * 32) : (VT)0;
+    for (int u = 0; u < CH; ++u) aa[u] = jj + u < len ? ld_val(vp + (long long)(jj + u) * 32) : (VT)0;
     XT xv[CH][R];
 #pragma unroll
     for (int u = 0; u < CH; ++u)
@@ -370,7 +417,22 @@ struct ColStage {
     __syncwarp();
   }
 
-  // stage k <- columns of slice s (lane 0 issues; warp-uniform bookkeeping)
+  // Per warp: the vector whose slice rows the current pass's row epilogue
+  // reads and the gathers of x do not bring into cache (set by lane 0 at the
+  // start of a pass, read by lane 0 when it issues a slice), or null.  Kept
+  // in shared memory rather than a register: the SpMV loop is register-bound.
+  __device__ __forceinline__ static const void** row_pf_slot() {
+    __shared__ const void* s_row_pf[32];
+    return s_row_pf + (threadIdx.x >> 5);
+  }
+
+  // stage k <- columns of slice s (lane 0 issues; warp-uniform bookkeeping).
+  // With RowB > 0 (bytes per row of the epilogue's vector) and a vector set
+  // in row_pf_slot(), that vector's 32 rows of the slice are prefetched into
+  // L2 with the values, so the epilogue's load after the slice's SpMV is an
+  // L2 hit instead of a full HBM round trip.  Rows of a slice are
+  // consecutive only without a row perm.
+  template <unsigned RowB = 0>
   __device__ void issue(const KParams& kp, int k, long long s, int lane) {
     if (cap <= 0) return;
     const long long base = kp.slice_off[s];
@@ -383,9 +445,22 @@ struct ColStage {
       tma_bulk_g2s(buf(k), kp.col + base, bytes, b);
       // the slice's values, which the warp reads right after the columns,
       // start their way from HBM into L2 now
-      if (kp.pf_vals)
+      if (kp.pf_vals) {
         tma_bulk_prefetch_l2(static_cast<const unsigned char*>(kp.val) + base * kp.pf_vals,
                              (unsigned)kp.pf_vals * 32u * (unsigned)len);
+        if constexpr (RowB > 0) {
+          const void* rp = *row_pf_slot();
+          if (rp && !kp.perm) {
+            // rows s*32 .. min(s*32 + 32, n) of an n-row buffer: the start is
+            // a multiple of 32 rows (aligned), the length rounded down to
+            // whole 16-byte units
+            const long long r0 = s * 32;
+            const long long nr = kp.n - r0 < 32 ? kp.n - r0 : 32;
+            const unsigned pb = nr > 0 ? (unsigned)(nr * RowB) & ~15u : 0u;
+            if (pb > 0) tma_bulk_prefetch_l2(static_cast<const unsigned char*>(rp) + r0 * RowB, pb);
+          }
+        }
+      }
     }
     st |= 4u << k;
   }
@@ -424,14 +499,22 @@ struct ColStage {
 };
 
 // One SpMV pass over the block's slices: z = A x for the slice rows, then
-// epi(s, z) for the row epilogue.
+// epi(s, z) for the row epilogue.  rowpf: the [n][R] storage-precision
+// vector the epilogue reads at the slice rows and that the gathers of x do
+// not bring into cache (prefetched one slice ahead with the values when the
+// matrix streams from HBM), or null.
 template <class Pol, int R, class XT, class Epi>
 __device__ __forceinline__ bool spmv_pass(const KParams& kp, const Ctx& c, ColStage& cs, const XT* x, Epi&& epi,
-                                          PassSync* wait = nullptr) {
+                                          PassSync* wait = nullptr, const typename Pol::BT* rowpf = nullptr) {
   using AT = typename Pol::AT;
+  // (one and two right-hand sides: with four, the 1M-node FE disk's mixed
+  // launch measured 2.5% slower with the row prefetch, 3D 256^3 mixed with one
+  // right-hand side 2% faster)
+  constexpr unsigned kRowB = R <= 2 ? (unsigned)(R * sizeof(typename Pol::BT)) : 0u;
   const long long sb = kp.blk_slice[c.b()], se = kp.blk_slice[c.b() + 1];
   long long s = sb + c.warp();
-  if (s < se) cs.issue(kp, 0, s, c.lane());
+  if (kRowB > 0 && c.lane() == 0) *ColStage::row_pf_slot() = rowpf;
+  if (s < se) cs.issue<kRowB>(kp, 0, s, c.lane());
   // the ordering wait on the previous pass comes after the first column copy
   // is issued: the matrix does not depend on it, so the copy overlaps the wait
   if (wait && !wait->before_next(kp)) {
@@ -441,7 +524,7 @@ __device__ __forceinline__ bool spmv_pass(const KParams& kp, const Ctx& c, ColSt
   int k = 0;
   for (; s < se; s += c.nw(), k ^= 1) {
     const long long sn = s + c.nw();
-    if (sn < se) cs.issue(kp, k ^ 1, sn, c.lane());
+    if (sn < se) cs.issue<kRowB>(kp, k ^ 1, sn, c.lane());
     const int* scol = cs.ready(kp, k, c.lane());
     AT z[R];
     spmv_slot<Pol, R, XT>(kp, s, c.lane(), x, z, scol);
@@ -838,7 +921,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
 #pragma unroll
         for (int r = 0; r < R; ++r) { wh[r] = Pol::to_h(w[r]); apa[r] = Pol::dot(apa[r], w[r], sv[r]); }
         VecIO<R>::st(Hw + row * R, wh);
-      });
+      }, nullptr, j > 0 ? Wout : nullptr);
     } else {
       // Horner pass 1: u = gamma_1 v_j + A (gamma_0 v_j); stores v_j
       {
@@ -899,7 +982,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
 #pragma unroll
             for (int r = 0; r < R; ++r) u[r] = Pol::to_h(Pol::add_mul(z[r], sh.gr[h][r], sv[r]));
             VecIO<R>::st(hout + row * R, u);
-          }, &ps);
+          }, &ps, src);
           if (!ok) return false;
           ps.done(kp);
         }
@@ -924,7 +1007,7 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
 #pragma unroll
         for (int r = 0; r < R; ++r) { wh[r] = Pol::to_h(w[r]); apa[r] = Pol::dot(apa[r], w[r], sv[r]); }
         VecIO<R>::st(Hw + row * R, wh);
-      }, &ps);
+      }, &ps, j > 0 ? Wout : src);
       if (!ok) return false;
     }
     {
@@ -951,7 +1034,36 @@ __device__ bool phase_lanczos(const KParams& kp, const Ctx& c, const Grp& g, Pas
 #pragma unroll
       for (int r = 0; r < R; ++r) bpa[r] = Pol::zero();
       const bool ro = RO && kp.reorth > 0;
-      for (long long i = g.gt(kp); i < g.r1(kp); i += g.tt()) {
+      long long i = g.gt(kp);
+      if (!ro) {
+        // a pure stream (16-32 bytes per row): PB rows per thread per
+        // iteration with all their loads issued before any store, so each
+        // thread keeps PB rows in flight; rows and the ||w||^2 terms in the
+        // same order as the one-row loop below (bit-identical sums)
+        constexpr int PB = R == 1 ? 4 : (R == 2 ? 2 : 1);
+        const long long i1 = g.r1(kp), step = g.tt();
+        for (; PB > 1 && i + (PB - 1) * step < i1; i += PB * step) {
+          HT wh[PB][R];
+          BT v[PB][R];
+#pragma unroll
+          for (int u = 0; u < PB; ++u) {
+            VecIO<R>::ld(Hw + (i + u * step) * R, wh[u]);
+            VecIO<R>::ld(src + (i + u * step) * R, v[u]);
+          }
+#pragma unroll
+          for (int u = 0; u < PB; ++u) {
+            BT wb[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+              AT w = Pol::sub_mul(h_load_at<Pol>(wh[u][r]), sh.al[r], v[u][r]);
+              wb[r] = Pol::to_b(w);
+              bpa[r] = Pol::dot_self(bpa[r], w);
+            }
+            VecIO<R>::st(Wout + (i + u * step) * R, wb);
+          }
+        }
+      }
+      for (; i < g.r1(kp); i += g.tt()) {
         HT wh[R];
         BT wb[R], v[R];
         VecIO<R>::ld(Hw + i * R, wh);
