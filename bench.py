@@ -405,7 +405,8 @@ def run_ours(args, P, rank, world, local):
         # 250k-node adjoint with its finite-difference checks
         ke, we = max(3, min(K, 10)), max(3, min(W, 3))
         line["fd3d_256"] = _extra("fd3d_256", fd3d_measure, 256, ke, we)
-        line["batch_64"] = _extra("batch_64", batch_measure, ke, we, tune=False, monodomain=False)
+        line["fd2d_256"] = _extra("fd2d_256", fd2d_measure, 20, 5)
+        line["batch_64"] = _extra("batch_64", batch_measure, ke, we, tune=False, monodomain=True)
         if "mixed_batched_over_fp64_single" in line["batch_64"]:
             line["mixed_batched_over_plain_fp64"] = {
                 "batch_64": line["batch_64"]["mixed_batched_over_fp64_single"],
@@ -671,6 +672,45 @@ def _timed_solves(eng, stream, K, W):
         e1.record(stream)
         torch.cuda.synchronize()
     return e0.elapsed_time(e1) / K
+
+
+# Launch shape of the 256^2 FD solve when it is not autotuned: the one the
+# autotuner chose on GB300 (256-thread blocks, one block per SM, no column
+# staging, grid barriers between passes; the solve is latency-bound).
+FD2D_SHAPE = dict(threads=256, blocks_per_sm=1, col_staging=1, sync_policy=1)
+
+
+def fd2d_measure(K: int, W: int) -> dict:
+    """Config 1 (2D 5-point Dirichlet Laplacian on 256^2, FP64, m = 60,
+    C = 32, k = 10 analytic sine modes, no preconditioner): fused-launch
+    solves/s with the engine's default launch shape and with the autotuner's
+    shape, the error against the FP64 oracle, and against the exact DST-I
+    solution (the Krylov truncation error of m = 60, as in the reference)."""
+    import torch
+    from gpumatfun_gb300 import Engine, workloads
+    from oracle import fab, known
+    P = workloads.cached_problem("fd2d-256")
+    stream = torch.cuda.Stream()
+    out = {"config": {"workload": "fd2d-256", "n": int(P.n), "nnz": int(P.A.nnz), "m": P.m, "C": P.C, "d": P.d,
+                      "k": P.k, "nrhs": P.R, "precision": "fp64"}}
+    x = None
+    for tag, shape in (("default_shape", {}), ("autotuned_shape", FD2D_SHAPE)):
+        eng = Engine.from_problem(P, precision="fp64", sync=False, **shape)
+        ms = _timed_solves(eng, stream, K, W)
+        x = eng.get_solution()
+        info = eng.info()
+        eng.delete()
+        out[tag] = {"solves_per_s": P.R * 1e3 / ms, "ms_per_launch": ms, "grid_blocks": info["grid_blocks"],
+                    "threads": info["threads"], **({"shape": shape} if shape else {})}
+    ora = fab.OracleEngine(A=P.A, U0=P.U, Q=P.Q, m=P.m, gamma=P.gamma, gs_re=P.gs_re, gs_im=P.gs_im,
+                           flam=P.flam, wts=P.wts, shifts=P.shifts,
+                           col_scale=P.col_scale if P.col_scale is not None else np.ones(P.R))
+    want = ora.solve()
+    out["rel_err_vs_fp64_oracle"] = float(np.linalg.norm(x - want) / np.linalg.norm(want))
+    exact = known.dst_fab_2d(P.U[:, 0], int(P.meta["N"]), P.funcs[0], scale=float(P.meta["scale"]))
+    xr = x.reshape(P.n, -1)[:, 0]
+    out["rel_err_vs_exact_dst"] = float(np.linalg.norm(xr - exact) / np.linalg.norm(exact))
+    return out
 
 
 # Launch shape of the batch when it is not autotuned: the one the autotuner

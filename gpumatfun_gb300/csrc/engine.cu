@@ -887,8 +887,16 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
   if (a->col_staging < 0 || a->col_staging > 2) return fail(e, GM_ERR_ARG, "col_staging must be 0 (auto), 1 (off) or 2 (on)");
   long long max_len = 0;
   for (size_t q = 0; q + 1 < slice_off.size(); ++q) max_len = std::max(max_len, (slice_off[q + 1] - slice_off[q]) / 32);
-  // (val_prefetch = 1 forces the prefetch, which rides on the stages)
-  const bool staging = a->col_staging == 2 || (a->col_staging == 0 && (!use_window || a->val_prefetch == 1));
+  // (val_prefetch = 1 forces the prefetch, which rides on the stages).
+  // Since the SpMV walks one entry per step with the column source fixed per
+  // row, the FP64 engine gains from staging an L2-held matrix too (1M-node
+  // FE disk FP64 19.68 vs 21.18 ms per solve), where the mixed engine still
+  // loses (16.19 vs 14.94 ms): FP64 engines without matrix-powers passes
+  // (whose level-between vector shares the dynamic shared memory) stage
+  // whenever the slices fit a stage.
+  const bool stage_l2 = e->prec == GM_FP64 && !e->mpk_req;
+  const bool staging = a->col_staging == 2 ||
+                       (a->col_staging == 0 && (!use_window || a->val_prefetch == 1 || stage_l2));
   const int stage_cap = staging ? (int)std::min<long long>(max_len, 24) : 0;
   const size_t stage_smem = stage_cap > 0 ? (size_t)16 * (e->threads / 32) + (size_t)2 * (e->threads / 32) * stage_cap * 128 : 0;
   e->kp.stage_cap = stage_cap;
@@ -1326,7 +1334,7 @@ static int set_U_common(gm_handle h, const double* U, bool on_device) {
   if (rc) return rc;
   if (h->fe_cur == 0) h->fe_fwd_ok = false;   // the stored forward state is being replaced
   GM_CUDA(h, cudaMemsetAsync(h->kp.status, 0, sizeof(int), h->stream));
-  GM_CUDA(h, cudaMemsetAsync(h->kp.bar, 0, sizeof(unsigned), h->stream));
+  GM_CUDA(h, cudaMemsetAsync(h->kp.bar, 0, (2 + 2 * (size_t)h->nprob) * sizeof(unsigned), h->stream));
   h->have_V = h->have_y = h->have_coef = false;
   return launch(h, gm::PH_DEFLATE, 0);
 }
@@ -1347,7 +1355,7 @@ int gm_set_state(gm_handle h, const double* Usol_host, const double* ode_host) {
   if (rc) return rc;
   if (h->fe_cur == 0) h->fe_fwd_ok = false;
   GM_CUDA(h, cudaMemsetAsync(h->kp.status, 0, sizeof(int), h->stream));
-  GM_CUDA(h, cudaMemsetAsync(h->kp.bar, 0, sizeof(unsigned), h->stream));
+  GM_CUDA(h, cudaMemsetAsync(h->kp.bar, 0, (2 + 2 * (size_t)h->nprob) * sizeof(unsigned), h->stream));
   h->have_V = h->have_y = h->have_coef = false;
   return launch(h, gm::PH_DEFLATE, 0);
 }

@@ -74,7 +74,7 @@ struct KParams {
   double* tri;
   double* Z;
   double* part;     // [2R + k R][G]
-  unsigned* bar;    // [0] count, [1] generation
+  unsigned* bar;    // 64-bit barrier arrival counters: [0,1] whole grid, [2+2p, 3+2p] group p
   const int* blk_slice;       // [G+1] slice range owned by each block
   const int* dep_ptr;         // [G+1] neighbour list of each block
   const int* dep_idx;
@@ -144,6 +144,12 @@ struct PassSync {
   __device__ bool before_next(const KParams& kp);
 };
 
+// Arrival counter of problem group p's barrier (words 2 + 2p, 3 + 2p of
+// kp.bar), or of the whole grid's (words 0, 1) for p = -1.
+__device__ __forceinline__ unsigned long long* bar_word(const KParams& kp, int p) {
+  return reinterpret_cast<unsigned long long*>(kp.bar + 2 + 2 * p);
+}
+
 // The block's problem group.  A launch can carry several independent
 // problems (a batch); each owns a contiguous range of blocks, rows and SELL
 // slices, its own barrier and its own reductions.  One problem is the
@@ -169,13 +175,13 @@ struct Grp {
   __device__ __forceinline__ long long tt() const { return (long long)Gp * blockDim.x; }
   // barrier over this group's blocks (words 2 + 2p, 3 + 2p of kp.bar)
   __device__ GridBar bar(const KParams& kp) const {
-    return GridBar{kp.bar + 2 + 2 * p, kp.bar + 3 + 2 * p, kp.status, (unsigned)Gp, kp.timeout_ns};
+    return GridBar{bar_word(kp, p), kp.status, (unsigned)Gp, kp.timeout_ns};
   }
 };
 
 __device__ __forceinline__ GridBar group_bar(const KParams& kp, int p) {
   const unsigned Gp = kp.nprob > 0 ? (unsigned)(kp.prob_blk0[p + 1] - kp.prob_blk0[p]) : (unsigned)kp.G;
-  return GridBar{kp.bar + 2 + 2 * p, kp.bar + 3 + 2 * p, kp.status, Gp, kp.timeout_ns};
+  return GridBar{bar_word(kp, p), kp.status, Gp, kp.timeout_ns};
 }
 
 __device__ __forceinline__ bool PassSync::before_next(const KParams& kp) {
@@ -296,6 +302,7 @@ __device__ __forceinline__ void spmv_slot(const KParams& kp, long long s, int la
       row_entries1<Pol, R, XT, false>((colarr ? colarr : kp.col) + base + lane, vp, len, x, dl, acc);
     return;
   }
+  // Chunks of two or more entries (two right-hand sides; tuning builds).
   // Column indices from the shared-memory stage when the slice is staged,
   // else from global memory, chosen by a warp-uniform branch per chunk;
   // values from global memory (read-only path; with value prefetch they are
@@ -1259,9 +1266,10 @@ __device__ bool phase_apply(const KParams& kp, const Ctx& c, const Grp& g, bool 
       for (int ii = 0; ii < IC; ++ii)
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[ii][r] = Pol::zero();
-      for (int q = 0; q < m; ++q) {
-        BT v[R];
-        VecIO<R>::ld(V + ((long long)q * n + i) * R, v);
+      // acc[ii] += c_{i0+ii}[q] V_q[i] over the basis, q ascending.  V
+      // streams from HBM once (m rows of n R entries): QU basis rows are
+      // loaded before they are used, so each warp keeps QU loads in flight
+      auto lift = [&](int q, const BT (&v)[R]) {
 #pragma unroll
         for (int ii = 0; ii < IC; ++ii) {
           if (i0 + ii < d1) {
@@ -1277,6 +1285,20 @@ __device__ bool phase_apply(const KParams& kp, const Ctx& c, const Grp& g, bool 
             }
           }
         }
+      };
+      constexpr int QU = R == 1 ? 8 : (R == 2 ? 4 : 2);
+      int q = 0;
+      for (; q + QU <= m; q += QU) {
+        BT v[QU][R];
+#pragma unroll
+        for (int u = 0; u < QU; ++u) VecIO<R>::ld(V + ((long long)(q + u) * n + i) * R, v[u]);
+#pragma unroll
+        for (int u = 0; u < QU; ++u) lift(q + u, v[u]);
+      }
+      for (; q < m; ++q) {
+        BT v[R];
+        VecIO<R>::ld(V + ((long long)q * n + i) * R, v);
+        lift(q, v);
       }
       if (d == 0) {
         double x[R], u[R], s[R];
@@ -1352,7 +1374,7 @@ template <int R>
 __device__ bool phase_deflate(const KParams& kp, const Ctx& c, int mode) {
   const long long n = kp.n;
   const int k = kp.k, G = kp.G;
-  GridBar bar{kp.bar, kp.bar + 1, kp.status, (unsigned)G, kp.timeout_ns};
+  GridBar bar{bar_word(kp, -1), kp.status, (unsigned)G, kp.timeout_ns};
   double* part_z = kp.part + 2LL * R * G;
   constexpr int KC = 4;
   if (mode != 0 && R == 2) {
@@ -1494,7 +1516,7 @@ __global__ void __launch_bounds__(GM_MAXT, (R >= 4 ? ((Pol::kMixed && !(PH & (PH
   bool first = true;
   auto sep = [&]() -> bool {
     if (first) { first = false; return true; }
-    return GridBar{kp.bar, kp.bar + 1, kp.status, (unsigned)kp.G, kp.timeout_ns}.sync();
+    return GridBar{bar_word(kp, -1), kp.status, (unsigned)kp.G, kp.timeout_ns}.sync();
   };
   if ((PH & PH_LANCZOS) && (ph & PH_LANCZOS)) {
     if (!sep()) return;

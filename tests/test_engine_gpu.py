@@ -291,20 +291,22 @@ def test_sync_policies_agree(engine_lib, degree):
 
 def test_info_ex_reports_l2_window_and_staging(engine_lib):
     """gm_info_ex: the L2 window and the column staging each engine chose
-    (auto: window when the matrix and one pass's vectors fit L2, staging only
-    without a window), and a count below the total fills only that many."""
+    (auto: window when the matrix and one pass's vectors fit L2; staging
+    without a window, and with one in the FP64 engine but not in the mixed
+    one), and a count below the total fills only that many."""
     import ctypes as ct
     P = workloads.fd2d_problem(64, 2, 24, 24, [params.frac_exp(1e-3, 1.5)], R=1, scale=65.0 ** 2, seed=3)
-    mat_bytes = 8 * P.A.nnz
-    for win, stg in ((0, 0), (1, 0), (2, 0), (1, 2)):
-        eng = Engine.from_problem(P, l2_window=win, col_staging=stg)
+    for prec, win, stg in (("fp64", 0, 0), ("fp64", 1, 0), ("fp64", 2, 0), ("fp64", 1, 2), ("fp64", 0, 1),
+                           ("mixed", 0, 0), ("mixed", 1, 0)):
+        mat_bytes = (8 if prec == "fp64" else 4) * P.A.nnz
+        eng = Engine.from_problem(P, precision=prec, l2_window=win, col_staging=stg)
         info = eng.info()
         if win == 1:
             assert info["l2_window_bytes"] == 0
             assert (info["col_stage_groups"] > 0) == (stg in (0, 2))
         else:
             assert info["l2_window_bytes"] >= mat_bytes
-            assert info["col_stage_groups"] == 0
+            assert (info["col_stage_groups"] > 0) == (prec == "fp64" and stg == 0)
         v = (ct.c_int64 * 19)(*([-7] * 19))
         assert engine_lib.gm_info_ex(eng._h, v, 3) == 0
         assert list(v)[:3] == [P.n, 1, P.m] and list(v)[3:] == [-7] * 16
