@@ -1266,10 +1266,9 @@ __device__ bool phase_apply(const KParams& kp, const Ctx& c, const Grp& g, bool 
       for (int ii = 0; ii < IC; ++ii)
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[ii][r] = Pol::zero();
-      // acc[ii] += c_{i0+ii}[q] V_q[i] over the basis, q ascending.  V
-      // streams from HBM once (m rows of n R entries): QU basis rows are
-      // loaded before they are used, so each warp keeps QU loads in flight
-      auto lift = [&](int q, const BT (&v)[R]) {
+      for (int q = 0; q < m; ++q) {
+        BT v[R];
+        VecIO<R>::ld(V + ((long long)q * n + i) * R, v);
 #pragma unroll
         for (int ii = 0; ii < IC; ++ii) {
           if (i0 + ii < d1) {
@@ -1285,20 +1284,6 @@ __device__ bool phase_apply(const KParams& kp, const Ctx& c, const Grp& g, bool 
             }
           }
         }
-      };
-      constexpr int QU = R == 1 ? 8 : (R == 2 ? 4 : 2);
-      int q = 0;
-      for (; q + QU <= m; q += QU) {
-        BT v[QU][R];
-#pragma unroll
-        for (int u = 0; u < QU; ++u) VecIO<R>::ld(V + ((long long)(q + u) * n + i) * R, v[u]);
-#pragma unroll
-        for (int u = 0; u < QU; ++u) lift(q + u, v[u]);
-      }
-      for (; q < m; ++q) {
-        BT v[R];
-        VecIO<R>::ld(V + ((long long)q * n + i) * R, v);
-        lift(q, v);
       }
       if (d == 0) {
         double x[R], u[R], s[R];
