@@ -16,12 +16,13 @@ CSRC = PKG / "csrc"
 LIBDIR = PKG / "_lib"
 LIB = Path(os.environ["GPUMATFUN_LIB"]) if os.environ.get("GPUMATFUN_LIB") else LIBDIR / "libgpumatfun.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["engine.cu", "kern_fp64.cu", "kern_mixed.cu", "noalloc.cu", "eigs.cu"]
+SOURCES = ["engine.cu", "kern_fp64.cu", "kern_mixed.cu", "kern_mixed_l2.cu", "noalloc.cu", "eigs.cu"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC"]
 # Kernel shape overrides for tuning builds, e.g. "-DGM_MINB1=2 -DGM_CH1=4"
 # (GM_MINB1 / GM_MINB / GM_MINB4: minimum resident 512-thread blocks per SM
 # for 1 / 2 / 4 right-hand sides; GM_MINB1X: one right-hand side, matrix-powers
-# and Gram-Schmidt entry points; GM_MINB4M: four right-hand sides, mixed
+# and Gram-Schmidt entry points; GM_MINB1L2: one right-hand side, mixed, with
+# the matrix in the L2 window; GM_MINB4M: four right-hand sides, mixed
 # precision; GM_CH1/2/4/4F: SpMV chunk width for 1/2/4 right-hand sides, 4F the
 # FP32-stored mixed engine).
 EXTRA = os.environ.get("GPUMATFUN_NVCC_EXTRA", "").split()

@@ -24,6 +24,7 @@ using gm::KParams;
 namespace gm {
 void* kernel_fp64(int R, int group);
 void* kernel_mixed(int R, int group);
+void* kernel_mixed_l2(int group);
 }  // namespace gm
 
 namespace {
@@ -609,9 +610,22 @@ void window_release(int dev) {
   }
 }
 
-void* pick_kernel(int prec, int R, int group) {
+// l2: a mixed engine's matrix is held in the L2 persisting window; one
+// right-hand side then runs the SpMV groups compiled for two resident blocks
+// per SM (gm::PolMixedL2, no register spills).
+void* pick_kernel(int prec, int R, int group, bool l2) {
+  if (l2 && R == 1 && prec != GM_FP64) {
+    void* k = gm::kernel_mixed_l2(group);
+    if (k) return k;
+  }
   return prec == GM_FP64 ? gm::kernel_fp64(R, group) : gm::kernel_mixed(R, group);
 }
+
+// Tuning builds: -DGM_L2K_MIXED=0 keeps the three-block kernels for an
+// L2-held matrix.
+#ifndef GM_L2K_MIXED
+#define GM_L2K_MIXED 1
+#endif
 
 int group_of(int phases) {
   const int solve = gm::PH_TRISOLVE | gm::PH_COEF;
@@ -909,12 +923,13 @@ int create_impl(const gm_create_args* a, const std::vector<ProbIn>& probs, gm_en
   // warp: small problems get fewer blocks, which makes every grid barrier
   // cheaper).  The matrix-powers and Gram-Schmidt groups, compiled for fewer
   // resident blocks, bound the grid only of engines that launch them.
+  const bool l2k = use_window && e->prec != GM_FP64 && GM_L2K_MIXED != 0;
   const long long nsl = (long long)slice_off.size() - 1;
   const int nw = e->threads / 32;
   const long long want = std::max<long long>(np, (nsl + nw - 1) / nw);
   long long Gmax = 0;
   for (int g = 0; g < KGRP_N; ++g) {
-    e->kfn[g] = pick_kernel(e->prec, e->R, g);
+    e->kfn[g] = pick_kernel(e->prec, e->R, g, l2k);
     if (!e->kfn[g]) return fail(e, GM_ERR_UNSUPPORTED, "no kernel for nrhs %d", e->R);
     e->smem[g] = (g == KGRP_LANCZOS || g == KGRP_APPLY || g == KGRP_FUSED || g == KGRP_LANCZOS_MPK ||
                   g == KGRP_FUSED_MPK || g == KGRP_LANCZOS_RO || g == KGRP_FUSED_RO) ? stage_smem : 0;

@@ -114,6 +114,7 @@ struct PolFP64 {
   using AT = double;   // per-element accumulator
   using ST = double;   // scalar used in per-element operations
   static constexpr bool kMixed = false;
+  static constexpr bool kL2 = false;
   __device__ static __forceinline__ AT zero() { return 0.0; }
   __device__ static __forceinline__ ST scalar(double s) { return s; }
   __device__ static __forceinline__ AT acc(AT a, VT v, double x) { return fma(v, x, a); }
@@ -140,6 +141,7 @@ struct PolMixed {
   using AT = ff;
   using ST = ff;
   static constexpr bool kMixed = true;
+  static constexpr bool kL2 = false;
   __device__ static __forceinline__ AT zero() { return {0.f, 0.f}; }
   __device__ static __forceinline__ ST scalar(double s) { return ff_from_double(s); }
   // SpMV row accumulation: hi gathers the exactly-split products (two_sum),
@@ -200,6 +202,17 @@ struct PolMixed {
     return p.hi + p.lo;
   }
 };
+
+// The mixed arithmetic for one-right-hand-side kernels compiled at two
+// resident 512-thread blocks per SM (64 registers, no spills) instead of
+// three (40 registers).  Mixed engines whose matrix is held in the L2
+// persisting window use them: there the spill frames of the 40-register build
+// compete with the vectors for the L2 left beside the window (1M-node FE disk:
+// 13.9 vs 14.5 ms per solve), while a matrix streamed from HBM wants the third
+// block's loads in flight (3D 256^3: 44.6 vs 37.8 ms with two blocks).  The
+// FP64 engine, which spills little at 40 registers, measured slower with two
+// blocks on the same L2-held disk (21.2 vs 19.2 ms) and has no such variant.
+struct PolMixedL2 : PolMixed { static constexpr bool kL2 = true; };
 
 __device__ __forceinline__ double h_to_d(double h) { return h; }
 __device__ __forceinline__ double h_to_d(float2 h) { return (double)h.x + (double)h.y; }

@@ -380,9 +380,14 @@ __device__ __forceinline__ void spmv_slot(const KParams& kp, long long s, int la
   }
 }
 
-template <class Pol> __device__ __forceinline__ typename Pol::AT h_load_at(const typename Pol::HT& h);
-template <> __device__ __forceinline__ double h_load_at<PolFP64>(const double& h) { return h; }
-template <> __device__ __forceinline__ ff h_load_at<PolMixed>(const float2& h) { return {h.x, h.y}; }
+// A Horner / lift buffer entry as the policy's accumulator.
+template <class Pol> __device__ __forceinline__ typename Pol::AT h_load_at(const typename Pol::HT& h) {
+  if constexpr (Pol::kMixed) {
+    return {h.x, h.y};
+  } else {
+    return h;
+  }
+}
 
 // Per-warp double-buffered staging of SELL column indices.  Lane 0 issues a
 // TMA bulk copy of the next slice's column block (128 bytes per slice column,
@@ -1488,8 +1493,12 @@ template <class Pol, int R, int PH>
 #ifndef GM_MINB1X
 #define GM_MINB1X 2   // one right-hand side, matrix-powers or Gram-Schmidt entry points
 #endif
+#ifndef GM_MINB1L2
+#define GM_MINB1L2 2   // one right-hand side, mixed, matrix held in the L2 window (PolMixedL2)
+#endif
 __global__ void __launch_bounds__(GM_MAXT, (R >= 4 ? ((Pol::kMixed && !(PH & (PH_MPK | PH_REORTH))) ? GM_MINB4M : GM_MINB4)
-                                            : (R == 1 ? ((PH & (PH_MPK | PH_REORTH)) ? GM_MINB1X : GM_MINB1)
+                                            : (R == 1 ? ((PH & (PH_MPK | PH_REORTH)) ? GM_MINB1X
+                                                                                     : (Pol::kL2 ? GM_MINB1L2 : GM_MINB1))
                                                       : GM_MINB))) fab_kernel(KParams kp) {
   const Ctx c(kp.G);
   if (*(volatile int*)kp.status != 0) return;
